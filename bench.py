@@ -1,0 +1,442 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300-native barotropic time step (one JSON line).
+
+Default workload (the metric's headline configuration): a 64-member FP32
+ensemble in one batch -- 16 x 180x91 (dt 480 s), 32 x 360x181 (dt 240 s),
+16 x 720x361 (dt 120 s), one model day each -- from the seeded harmonic
+state (gd0 = 8000 m g, degree 1..6, 100 m / 1e7 m^2 s^-1 RMS) plus
+N(0, 1 m) g white noise per member.  Scheme: predict_correct, csp2 with 6
+subcycles, qcon_modified, center_diff, zonal filter cutoff 4 on the rows
+within ~5 degrees of each pole.  A "step" is one model step of every active
+member; --steps 720 (default) is the whole job.  `value` is grid-point
+steps per second over the timed steps with the inputs resident in HBM; the
+plain FP64 path (360x181, 360 steps) is timed beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload batch|plain|serve]
+
+--impl reference times the CPU oracle (the restatement of the reference's
+Fortran, which cannot be built here) on the host cores over a bounded
+sample of the same ensemble.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+for _p in (ROOT, ROOT / "gamil-dycore_gb300"):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
+
+G = 9.80616
+# grid -> (num_lon, num_lat, dt, steps per model day, filter cutoffs)
+GRIDS = {
+    180: (180, 91, 480.0, 180, [4] * 3),
+    360: (360, 181, 240.0, 360, [4] * 5),
+    720: (720, 361, 120.0, 720, [4] * 10),
+    1440: (1440, 721, 60.0, 1440, [4] * 20),
+}
+ENSEMBLE = [(180, 16), (360, 32), (720, 16)]
+
+
+def peaks():
+    try:
+        return json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        return {}
+
+
+def scheme(gdc, precision, subcycles=6):
+    return gdc.default_params(num_lon=360, num_lat=181, time_step_size=240.0, subcycles=subcycles,
+                              split_scheme=gdc.SPLIT_CSP2, qcon_modified=1, uv_adv_scheme=gdc.ADV_CENTER_DIFF,
+                              use_zonal_tend_filter=1, zonal_tend_filter_cutoff_wavenumber=[4] * 5,
+                              precision=precision)
+
+
+def ensemble_ics(gdc):
+    """Per-member initial states of the 64-member ensemble (host arrays)."""
+    base = {g: gdc.ic_seeded(GRIDS[g][0], GRIDS[g][1], seed=0) for g, _ in ENSEMBLE}
+    members = []
+    k = 0
+    for g, count in ENSEMBLE:
+        N, M, dt, nsteps, cut = GRIDS[g]
+        for _ in range(count):
+            u, v, gd, ghs = base[g]
+            gd = gdc.ic_add_noise(gd.copy(), N, M, seed=1000 + k, sigma=1.0 * G)
+            members.append(dict(N=N, M=M, dt=dt, nsteps=nsteps, cutoff=cut, ic=(u, v, gd, ghs)))
+            k += 1
+    return members
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9:
+                    rows.append(f)
+        except Exception:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except Exception:
+                pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        load = [s for s in sm if s > 0.5 * (max(mx) if mx else 2070)] or sm
+        return {"sm_mhz": statistics.median(load) if load else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup(n_gpus):
+    if n_gpus <= 1 or "RANK" not in os.environ:
+        return 0, 1, None
+    import torch
+    import torch.distributed as dist
+    rank, world = int(os.environ["RANK"]), int(os.environ["WORLD_SIZE"])
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)))
+    dist.init_process_group("nccl")
+    return rank, world, dist
+
+
+def reduce_max(dist, x: float) -> float:
+    """Max over ranks (replicas): the job is done when the slowest replica is."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# ------------------------------------------------------------------ ours
+
+def time_batch(gdc, torch, members, steps, warmup, precision, ts):
+    """Warm up, then time `steps` model steps of the whole ensemble with CUDA
+    events on the stream the kernels are launched on."""
+    b = gdc.Batch(scheme(gdc, precision))
+    b.set_stream(ts.cuda_stream)
+    ids = []
+    for m in members:
+        ids.append(b.add(m["N"], m["M"], m["dt"], warmup + m["nsteps"], *m["ic"], cutoff=m["cutoff"]))
+    b.step(warmup)
+    b.sync()
+    gpt = sum(m["N"] * m["M"] * min(steps, m["nsteps"]) for m in members)
+    launches_per_step = 4 * (6 + 2) + 1
+    active_steps = sum(min(steps, m["nsteps"]) for m in members)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(ts)
+    b.step(steps)
+    e1.record(ts)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    b.sync()
+    nan = [b.info(i)[2] for i in ids]
+    b.close()
+    return ms, gpt, launches_per_step * max(min(steps, m["nsteps"]) for m in members), active_steps, nan
+
+
+def e2e_batch(gdc, torch, members, steps, precision):
+    """The same job through the C ABI from host buffers: admit (H2D), step,
+    read every member's state back (D2H), all inside the timed region."""
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b = gdc.Batch(scheme(gdc, precision))
+    ids = [b.add(m["N"], m["M"], m["dt"], min(steps, m["nsteps"]), *m["ic"], cutoff=m["cutoff"]) for m in members]
+    b.step(steps)
+    b.sync()
+    outs = [b.get_state(i) for i in ids]
+    t1 = time.perf_counter()
+    b.close()
+    h2d = sum(sum(a.nbytes for a in m["ic"]) for m in members)
+    d2h = sum(sum(a.nbytes for a in o) for o in outs)
+    gpt = sum(m["N"] * m["M"] * min(steps, m["nsteps"]) for m in members)
+    return (t1 - t0) * 1e3, gpt, h2d, d2h
+
+
+def profile_kernels(gdc, members, precision, nsteps=2):
+    """Per-kernel-kind device time, launch by launch with CUDA events."""
+    b = gdc.Batch(scheme(gdc, precision))
+    for m in members:
+        b.add(m["N"], m["M"], m["dt"], nsteps + 1, *m["ic"], cutoff=m["cutoff"])
+    b.step(1)  # module load, attributes
+    b.sync()
+    ms, n = b.profile(nsteps)
+    b.close()
+    return ms, n
+
+
+def plain_fp64(gdc, torch, ts, steps=360):
+    """Config 0 through the plain FP64 path (one member, 360 steps)."""
+    N, M, dt, _, cut = GRIDS[360]
+    ic = gdc.ic_seeded(N, M, seed=0)
+    p = gdc.default_params(num_lon=N, num_lat=M, time_step_size=dt, subcycles=6, split_scheme=gdc.SPLIT_CSP2,
+                           qcon_modified=1, zonal_tend_filter_cutoff_wavenumber=cut, precision=gdc.FP64)
+    out = {}
+    for prec in (gdc.FP64, gdc.FP32):
+        p.precision = prec
+        m = gdc.Model(p)
+        m.set_stream(ts.cuda_stream)
+        m.set_state(*ic)
+        m.run(3)
+        m.set_state(*ic)
+        m.run(1)
+        m.set_state(*ic)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(ts)
+        m.step(steps)
+        e1.record(ts)
+        torch.cuda.synchronize()
+        m.sync()
+        out[prec] = (e0.elapsed_time(e1), m.get_state())
+        m.close()
+    import numpy as np
+    def rl2(a, b):
+        x, y = a[2:-2, 2:-2], b[2:-2, 2:-2]
+        return float(np.sqrt(np.sum((x - y) ** 2) / np.sum(y * y)))
+    s64, s32 = out[gdc.FP64][1], out[gdc.FP32][1]
+    return {"value": N * M * steps / (out[gdc.FP64][0] / 1e3), "ms": out[gdc.FP64][0],
+            "fp32_value": N * M * steps / (out[gdc.FP32][0] / 1e3),
+            "l2_fp32_vs_fp64": {"gd": rl2(s32[2], s64[2]), "u": rl2(s32[0], s64[0]), "v": rl2(s32[1], s64[1])}}
+
+
+def cpu_baseline_sample(seconds_target=12.0):
+    """The oracle (port of the reference, 1 thread) on a 360x181 member."""
+    import gdc
+    from oracle.oracle import OracleModel
+    N, M, dt, _, cut = GRIDS[360]
+    ic = gdc.ic_seeded(N, M, seed=0)
+    o = OracleModel(N, M, dt, subcycles=6, split_scheme=2, qcon_modified=1, cutoff=cut)
+    o.set_state(*ic)
+    t0 = time.perf_counter()
+    o.step(2)
+    per = (time.perf_counter() - t0) / 2
+    n = max(2, int(seconds_target / per))
+    t0 = time.perf_counter()
+    o.step(n)
+    t = time.perf_counter() - t0
+    return {"value": N * M * n / t, "unit": "grid-pt-steps/s", "cores": 1, "kind": "port",
+            "sample": f"oracle (C restatement of the reference, FP64, 1 thread): one 360x181 member, {n} csp2 steps"}
+
+
+def run_ours(args, rank, world, dist):
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    import gdc
+    torch.cuda.init()
+    ts = torch.cuda.Stream()
+    members = ensemble_ics(gdc)
+    if args.profile_only:
+        # Short run of the batched step for profilers (ncu launch lists).
+        b = gdc.Batch(scheme(gdc, gdc.FP32))
+        for m in members:
+            b.add(m["N"], m["M"], m["dt"], args.warmup + args.steps, *m["ic"], cutoff=m["cutoff"])
+        b.step(args.warmup + args.steps)
+        b.sync()
+        b.close()
+        return
+    pk = peaks()
+    # Warm the FP32 kernels and the FP64 plain path before anything is timed.
+    barrier(dist)
+    with Clocks(int(os.environ.get("LOCAL_RANK", 0))) as clk:
+        ms, gpt, launches, active_steps, nan = time_batch(gdc, torch, members, args.steps, args.warmup,
+                                                          gdc.FP32, ts)
+    clocks = clk.summary()
+    ms_all = reduce_max(dist, ms)
+    value = world * gpt / (ms_all / 1e3)
+    plain = plain_fp64(gdc, torch, ts)
+    e2e_ms, e2e_gpt, h2d, d2h = e2e_batch(gdc, torch, members, args.steps, gdc.FP32)
+    e2e_ms = reduce_max(dist, e2e_ms)
+    prof_ms, prof_n = profile_kernels(gdc, members, gdc.FP32)
+    if rank != 0:
+        return
+    # Roofline of the dominant kernel (the fused stage kernel): algorithmic
+    # bytes per launch = 10 prognostic words per grid point (stages read+write
+    # 7, 13 and 10 words: 30 over 3 launches) x 4 bytes x active points.
+    cells = sum(m["N"] * m["M"] for m in members)
+    stage_ms = prof_ms[0] / max(prof_n[0], 1)
+    stage_bytes = 10 * 4 * cells
+    achieved = stage_bytes / (stage_ms / 1e3) / 1e9
+    hbm = pk.get("hbm_gbs")
+    peak_src = "measured" if hbm else "fallback"
+    hbm = hbm or 6800.0
+    algo_bytes = 312 * 4  # 39 words x (6 + 2) predict_correct calls per grid-point-step
+    line = {
+        "metric": "grid-pt-steps/s batched FP32 vs plain FP64 on GB300 @L2<=1e-5; p50/p99 latency",
+        "value": value,
+        "unit": "grid-pt-steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_all / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded spherical-harmonic states + per-member N(0,1 m) noise)",
+        "config": {"workload": "ensemble: 16x180x91@480s + 32x360x181@240s + 16x720x361@120s, one model day each, "
+                               "FP32 compensated, csp2 m=6, filter on",
+                   "members": len(members), "grid_pt_steps": gpt, "scheme": "predict_correct+csp2(6)+qcon",
+                   "l2_cache": "inputs larger than L2 (working set ~0.8 GB vs 129 MB L2)",
+                   "parallelism": f"replicas x{world}"},
+        "clocks": clocks,
+        "e2e": {"value": world * e2e_gpt / (e2e_ms / 1e3), "unit": "grid-pt-steps/s",
+                "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": None, "kernel": "stage_kernel<float>", "peak_source": peak_src,
+                     "stage_ms_per_launch": stage_ms, "bytes_per_launch": stage_bytes,
+                     "kernel_ms": {"stage": prof_ms[0], "final": prof_ms[1], "diag": prof_ms[2]},
+                     "kernel_launches": {"stage": prof_n[0], "final": prof_n[1], "diag": prof_n[2]},
+                     "whole_step_frac": (gpt / (ms / 1e3)) * algo_bytes / 1e9 / hbm},
+        "plain_fp64": {"value": plain["value"], "unit": "grid-pt-steps/s",
+                       "config": "360x181 dt 240 s, 360 steps, FP64, one member",
+                       "fp32_single_member_value": plain["fp32_value"],
+                       "l2_fp32_vs_fp64_after_1_day": plain["l2_fp32_vs_fp64"],
+                       "batched_fp32_over_plain_fp64": value / plain["value"]},
+        "nan_members": sum(1 for x in nan if x >= 0),
+        "cpu_baseline": cpu_baseline_sample(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------- reference
+
+def _ref_member(task):
+    import sys as _s
+    for p in task["paths"]:
+        if p not in _s.path:
+            _s.path.insert(0, p)
+    import gdc
+    from oracle.oracle import OracleModel
+    N, M, dt, nst, cut, seed = task["N"], task["M"], task["dt"], task["nsteps"], task["cutoff"], task["seed"]
+    u, v, gd, ghs = gdc.ic_seeded(N, M, seed=0)
+    gd = gdc.ic_add_noise(gd.copy(), N, M, seed=seed, sigma=1.0 * G)
+    o = OracleModel(N, M, dt, subcycles=6, split_scheme=2, qcon_modified=1, cutoff=cut)
+    o.set_state(u, v, gd, ghs)
+    o.step(nst)
+    return N * M * nst
+
+
+def run_reference(args, rank, world, dist):
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    import __graft_entry__
+    __graft_entry__.build()
+    cores = os.cpu_count() or 1
+    # Bounded sample of the ensemble: every member advances a few steps
+    # (sized so one round is a few seconds on the host cores).
+    per_grid = {180: 8, 360: 4, 720: 2}
+    tasks = []
+    k = 0
+    for g, count in ENSEMBLE:
+        N, M, dt, _, cut = GRIDS[g]
+        for _ in range(count):
+            tasks.append(dict(N=N, M=M, dt=dt, nsteps=per_grid[g], cutoff=cut, seed=1000 + k,
+                              paths=[str(ROOT), str(ROOT / "gamil-dycore_gb300")]))
+            k += 1
+    rounds = max(1, min(args.steps, 3))
+    warm = max(0, min(args.warmup, 1))
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        for _ in range(warm):
+            pool.map(_ref_member, tasks[:cores])
+        t0 = time.perf_counter()
+        done = 0
+        for _ in range(rounds):
+            done += sum(pool.map(_ref_member, tasks))
+        t = time.perf_counter() - t0
+    value = done / t
+    sample = (f"oracle port (FP64 C restatement of the reference), {cores} processes over the 64-member ensemble, "
+              f"{rounds} round(s) of 8/4/2 steps per 180x91/360x181/720x361 member")
+    print(json.dumps({
+        "impl": "reference",
+        "metric": "grid-pt-steps/s batched FP32 vs plain FP64 on GB300 @L2<=1e-5; p50/p99 latency",
+        "value": value, "unit": "grid-pt-steps/s", "higher_is_better": True, "n_gpus": world,
+        "steps": rounds, "warmup": warm, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "ensemble: 16x180x91@480s + 32x360x181@240s + 16x720x361@120s (bounded sample)"},
+        "cpu_baseline": {"value": value, "unit": "grid-pt-steps/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "grid-pt-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=720)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="batch", choices=["batch"])
+    ap.add_argument("--profile-only", action="store_true",
+                    help="run warmup+steps of the ensemble batch and exit (for ncu)")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    rank, world, dist = dist_setup(args.gpus) if args.impl == "ours" else (
+        int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), None)
+    if args.impl == "reference":
+        run_reference(args, rank, world, dist)
+    else:
+        run_ours(args, rank, world, dist)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,1317 @@
+// gdc_engine.cpp -- host engine behind the C ABI (include/gdc.h).
+//
+// A batch holds up to kSlots members, each with its own grid, time step and
+// length, all advanced by one sequence of kernel launches per model step:
+// the launches of the reference's time_integrate (src/dycore_mod.F90:
+// 654-752) for the scheme of the batch, each covering the work items of
+// every active member.  One model step is captured once into a CUDA graph
+// per time-level parity and replayed.  A single model (gdc_handle) is a
+// batch of one member.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "gdc_internal.h"
+
+namespace gdc {
+
+namespace {
+
+constexpr int kSlots = 1024;
+constexpr size_t kAlign = 256;
+
+size_t align_up(size_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
+
+bool uses_isp(const gdc_params& p) { return p.split_scheme == GDC_SPLIT_ISP; }
+
+// Byte layout of one member's device allocation.
+struct Layout {
+  size_t st[SL_N][3], lo[SL_N][3], td[TS_N][3], ghs, coef, twid, rowinfo, dcoef, total;
+};
+
+template <typename T>
+Layout make_layout(const gdc_params& p, int N, int M) {
+  Layout L;
+  const size_t full = (size_t)M * N, half = (size_t)(M - 1) * N;
+  const size_t fsz[3] = {full, full, half};
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off = align_up(off + bytes);
+    return o;
+  };
+  const bool isp = uses_isp(p), fp32 = sizeof(T) == 4;
+  for (int s = 0; s < SL_N; ++s)
+    for (int f = 0; f < 3; ++f) {
+      const bool need = s != SL_SAVED || isp;
+      L.st[s][f] = need ? take(fsz[f] * sizeof(T)) : (size_t)-1;
+      const bool level = s <= SL_SAVED;
+      L.lo[s][f] = (need && level && fp32) ? take(fsz[f] * sizeof(T)) : (size_t)-1;
+    }
+  for (int t = 0; t < TS_N; ++t)
+    for (int f = 0; f < 3; ++f)
+      L.td[t][f] = (t <= TS_NEW || isp) ? take(fsz[f] * sizeof(T)) : (size_t)-1;
+  L.ghs = take(full * sizeof(T));
+  L.coef = take(coef_words(M) * sizeof(T));
+  L.twid = take(2 * (size_t)N * sizeof(T));
+  L.rowinfo = take((size_t)M * sizeof(int));
+  L.dcoef = take((size_t)(3 * M) * sizeof(double));
+  L.total = off;
+  return L;
+}
+
+size_t member_bytes_for(const gdc_params& p, int N, int M) {
+  return p.precision == GDC_FP32 ? make_layout<float>(p, N, M).total
+                                 : make_layout<double>(p, N, M).total;
+}
+
+std::string cuda_msg(const char* what, cudaError_t e) {
+  return std::string(what) + ": " + cudaGetErrorString(e);
+}
+
+struct MemberRec {
+  bool used = false, active = false, finished = false, nan = false;
+  int N = 0, M = 0;
+  double dt = 0;
+  long long nsteps = 0, steps_done = 0, nan_step = -1;
+  int level = SL_L1;  // slot holding this member's state(old)
+  void* dmem = nullptr;
+  size_t bytes = 0;
+  std::vector<int> rowinfo;
+  std::vector<double> ic_u, ic_v;  // padded-layout u, v of the initial condition
+  int ic_ld = 0;
+};
+
+}  // namespace
+
+// Interface shared by the FP64 and FP32 engines.
+struct BatchIface {
+  virtual ~BatchIface() = default;
+  virtual int add(int N, int M, double dt, long long nsteps, const int* cutoff, const double* u,
+                  const double* v, const double* gd, const double* ghs, int ld, size_t reserve,
+                  int* id) = 0;
+  virtual int remove(int id) = 0;
+  virtual int step(int n) = 0;
+  virtual int sync() = 0;
+  virtual int member_info(int id, long long* steps, int* fin, long long* nan) = 0;
+  virtual int get_state(int id, double* u, double* v, double* gd, double* iu, double* iv,
+                        double* ig, int ld) = 0;
+  virtual int diag(int id, double* m, double* e, double* b) = 0;
+  virtual int active(int* n) = 0;
+  virtual int set_tile(int r, int c) = 0;
+  virtual int autotune(int* r, int* c, double* ms) = 0;
+  virtual int profile(int n, double* ms, long long* launches) = 0;
+  virtual int set_stream(void* s) = 0;
+  virtual int debug_tendency(int id, int pass, double* du, double* dv, double* dgd, int ld) = 0;
+  std::string err;
+};
+
+template <typename T>
+class Batch final : public BatchIface {
+ public:
+  explicit Batch(const gdc_params& p) : P(p) {}
+  ~Batch() override { release(); }
+
+  int init() {
+    cudaError_t e = cudaSetDevice(P.device);
+    if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("cudaSetDevice", e));
+    e = cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("cudaStreamCreate", e));
+    stream = own_stream;
+    if (int rc = dalloc((void**)&d_mem, sizeof(MemberDev<T>) * kSlots)) return rc;
+    if (int rc = dalloc((void**)&d_counters, sizeof(unsigned) * kSlots)) return rc;
+    if (int rc = dalloc((void**)&d_beta, sizeof(double) * kSlots)) return rc;
+    if (int rc = dalloc((void**)&d_diag, sizeof(double) * 3 * kSlots)) return rc;
+    if (int rc = dalloc((void**)&d_steps, sizeof(long long) * kSlots)) return rc;
+    if (int rc = dalloc((void**)&d_nan, sizeof(long long) * kSlots)) return rc;
+    cudaMemset(d_counters, 0, sizeof(unsigned) * kSlots);
+    cudaMemset(d_beta, 0, sizeof(double) * kSlots);
+    cudaMemset(d_diag, 0, sizeof(double) * 3 * kSlots);
+    cudaMemset(d_steps, 0, sizeof(long long) * kSlots);
+    cudaMemset(d_nan, 0xff, sizeof(long long) * kSlots);  // -1
+    recs.resize(kSlots);
+    hdesc.resize(kSlots);
+    std::memset(hdesc.data(), 0, sizeof(MemberDev<T>) * kSlots);
+    tile_r = 8;
+    tile_c = 32;
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("init", e));
+    return GDC_OK;
+  }
+
+  // ------------------------------------------------------------ members
+  int add(int N, int M, double dt, long long nsteps, const int* cutoff, const double* u,
+          const double* v, const double* gd, const double* ghs, int ld, size_t reserve,
+          int* id) override {
+    if (N < 8 || M < 5 || ld < N + 4 || !(dt > 0) || nsteps < 0 || !u || !v || !gd || !ghs)
+      return fail(GDC_E_CONFIG, "add: invalid grid, time step, length or buffers");
+    gdc_params mp = P;  // this member's filter rows
+    if (cutoff)
+      for (int k = 0; k < 20; ++k) mp.zonal_tend_filter_cutoff_wavenumber[k] = cutoff[k];
+    for (int k = 0; k < 20; ++k) {
+      const int c = mp.zonal_tend_filter_cutoff_wavenumber[k];
+      if (c < 0 || 2 * (c + 1) >= N || 2 * (c + 1) > 120)
+        return fail(GDC_E_CONFIG, "zonal_tend_filter_cutoff_wavenumber out of range for this grid");
+    }
+    // Pole-row u must vanish: u(:,1) and u(:,num_lat) are never updated by
+    // the reference (update_state writes rows 2..num_lat-1 only), and every
+    // reference initial condition sets them to zero.
+    for (int jp : {0, M - 1})
+      for (int i = 0; i < N; ++i)
+        if (u[(size_t)(jp + 2) * ld + i + 2] != 0.0)
+          return fail(GDC_E_CONFIG, "pole-row u must be zero in the initial condition");
+    int slot = -1;
+    for (int s = 0; s < kSlots; ++s)
+      if (!recs[s].used) {
+        slot = s;
+        break;
+      }
+    if (slot < 0) return fail(GDC_E_OOM, "add: member table full");
+    const Layout L = make_layout<T>(P, N, M);
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    if (free_b < L.total + reserve) return fail(GDC_E_OOM, "add: not enough free device memory");
+    MemberRec& r = recs[slot];
+    r = MemberRec();
+    cudaError_t e = cudaMalloc(&r.dmem, L.total);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(GDC_E_OOM, cuda_msg("add: cudaMalloc", e));
+    }
+    r.used = true;
+    r.level = old_;
+    r.N = N;
+    r.M = M;
+    r.dt = dt;
+    r.nsteps = nsteps;
+    r.bytes = L.total;
+    // Host tables.
+    const Mesh mesh = make_mesh(N, M);
+    const Coef co = make_coef(mesh);
+    const int Mh = M - 1;
+    std::vector<T> coef(coef_words(M), T(0));
+    for (int j = 0; j < M; ++j) {
+      coef[cf_off(CF_COS, M) + j] = T(co.full_cos[j]);
+      coef[cf_off(CF_F, M) + j] = T(co.full_f[j]);
+      coef[cf_off(CF_C, M) + j] = T(co.full_c[j]);
+      coef[cf_off(CF_RADVLON, M) + j] = T(0.25 / co.full_dlon[j]);
+      coef[cf_off(CF_RADVLAT, M) + j] = T(0.25 / co.full_dlat[j]);
+      coef[cf_off(CF_DLON, M) + j] = T(co.full_dlon[j]);
+      coef[cf_off(CF_DLAT, M) + j] = T(co.full_dlat[j]);
+      if (j >= 1 && j <= M - 2) {
+        coef[cf_off(CF_C1, M) + j] = T(co.half_cos[j - 1] / co.full_cos[j]);
+        coef[cf_off(CF_C2, M) + j] = T(co.half_cos[j] / co.full_cos[j]);
+      }
+      coef[cf_off(CF_MASSW, M) + j] = T(co.full_cos[j] * mesh.dlon * mesh.dlat);
+    }
+    for (int j = 0; j < Mh; ++j) {
+      coef[ch_off(CH_COS, M) + j + 1] = T(co.half_cos[j]);
+      coef[ch_off(CH_RADVLON, M) + j + 1] = T(0.25 / co.half_dlon[j]);
+      coef[ch_off(CH_RADVLAT, M) + j + 1] = T(0.25 / co.half_dlat[j]);
+      coef[ch_off(CH_DLON, M) + j + 1] = T(co.half_dlon[j]);
+      coef[ch_off(CH_DLAT, M) + j + 1] = T(co.half_dlat[j]);
+    }
+    std::vector<T> twid(2 * (size_t)N);
+    for (int k = 0; k < N; ++k) {
+      twid[k] = T(std::cos(2.0 * kPi * k / N));
+      twid[N + k] = T(std::sin(2.0 * kPi * k / N));
+    }
+    std::vector<int> ff, kf, fh, kh;
+    make_filter_rows(mesh, mp, ff, kf, fh, kh);
+    r.rowinfo.assign(M, 0);
+    for (int j = 0; j < M; ++j) {
+      int bits = 0;
+      if (ff[j]) bits |= RI_FLAG_FULL;
+      if (j < Mh && fh[j]) bits |= RI_FLAG_HALF;
+      if (j == 0 || j == M - 1 || bits) bits |= RI_SPECIAL;
+      r.rowinfo[j] = bits | (kf[j] << 8) | ((j < Mh ? kh[j] : 0) << 20);
+    }
+    std::vector<double> dco(3 * (size_t)M, 0.0);
+    for (int j = 0; j < M; ++j) {
+      dco[j] = co.full_cos[j] * mesh.dlon * mesh.dlat;
+      dco[M + j] = co.full_cos[j];
+    }
+    for (int j = 0; j < Mh; ++j) dco[2 * M + j] = co.half_cos[j];
+    // iap_transform of the initial condition (src/types_mod.F90:399-426) in
+    // FP64 on the host, exactly as the reference evaluates it.
+    const size_t full = (size_t)M * N, half = (size_t)Mh * N;
+    std::vector<double> hg(full), hu(full), hv(half), hghs(full);
+    auto at = [&](const double* f, int i, int j) { return f[(size_t)(j + 2) * ld + (i + 2)]; };
+    std::vector<double> ig(full);
+    for (int j = 0; j < M; ++j)
+      for (int i = 0; i < N; ++i) {
+        hg[(size_t)j * N + i] = at(gd, i, j);
+        hghs[(size_t)j * N + i] = at(ghs, i, j);
+        ig[(size_t)j * N + i] = std::sqrt(at(gd, i, j));
+      }
+    for (int j = 0; j < M; ++j)
+      for (int i = 0; i < N; ++i) {
+        const int ip = (i + 1) % N;
+        hu[(size_t)j * N + i] = 0.5 * (ig[(size_t)j * N + i] + ig[(size_t)j * N + ip]) * at(u, i, j);
+      }
+    for (int j = 0; j < Mh; ++j)
+      for (int i = 0; i < N; ++i)
+        hv[(size_t)j * N + i] = 0.5 * (ig[(size_t)j * N + i] + ig[(size_t)(j + 1) * N + i]) * at(v, i, j);
+    r.ic_ld = ld;
+    r.ic_u.assign(u, u + (size_t)ld * (M + 4));
+    r.ic_v.assign(v, v + (size_t)ld * (Mh + 4));
+    // Descriptor.
+    MemberDev<T>& d = hdesc[slot];
+    std::memset(&d, 0, sizeof(d));
+    char* base = (char*)r.dmem;
+    d.N = N;
+    d.M = M;
+    d.Mh = Mh;
+    d.dt = dt;
+    d.pcdt[kAllPass] = dt;                   // integrator(time_step_size, ...)
+    d.pcdt[kFastPass] = dt / P.subcycles;    // fast_dt = time_step_size / subcycles
+    d.pcdt[kSlowPass] = 0.5 * dt;            // integrator(0.5 * time_step_size, ...)
+    for (int s = 0; s < SL_N; ++s)
+      for (int f = 0; f < 3; ++f) {
+        d.st[s][f] = L.st[s][f] == (size_t)-1 ? nullptr : (T*)(base + L.st[s][f]);
+        d.lo[s][f] = L.lo[s][f] == (size_t)-1 ? nullptr : (T*)(base + L.lo[s][f]);
+      }
+    for (int t = 0; t < TS_N; ++t)
+      for (int f = 0; f < 3; ++f) d.td[t][f] = L.td[t][f] == (size_t)-1 ? nullptr : (T*)(base + L.td[t][f]);
+    d.ghs = (T*)(base + L.ghs);
+    d.coef = (const T*)(base + L.coef);
+    d.twid = (const T*)(base + L.twid);
+    d.rowinfo = (const int*)(base + L.rowinfo);
+    d.dcoef = (const double*)(base + L.dcoef);
+    // Upload (synchronously: admission is a step-boundary operation).
+    sync_stream();
+    e = cudaMemset(r.dmem, 0, L.total);
+    if (e == cudaSuccess) e = cudaMemcpy(base + L.coef, coef.data(), coef.size() * sizeof(T), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(base + L.twid, twid.data(), twid.size() * sizeof(T), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(base + L.rowinfo, r.rowinfo.data(), M * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(base + L.dcoef, dco.data(), dco.size() * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = upload_field(d.ghs, nullptr, hghs);
+    const int lvl = old_;
+    if (e == cudaSuccess) e = upload_field(d.st[lvl][F_GD], d.lo[lvl][F_GD], hg);
+    if (e == cudaSuccess) e = upload_field(d.st[lvl][F_IU], d.lo[lvl][F_IU], hu);
+    if (e == cudaSuccess) e = upload_field(d.st[lvl][F_IV], d.lo[lvl][F_IV], hv);
+    if (e == cudaSuccess) e = cudaMemcpy(d_mem + slot, &d, sizeof(d), cudaMemcpyHostToDevice);
+    const long long minus1 = -1, zero = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(d_nan + slot, &minus1, sizeof(minus1), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_steps + slot, &zero, sizeof(zero), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      cudaFree(r.dmem);
+      r = MemberRec();
+      return fail(GDC_E_CUDA, cuda_msg("add: upload", e));
+    }
+    r.active = nsteps > 0;
+    r.finished = nsteps == 0;
+    dirty = true;
+    // diag_run of the initial state (src/dycore_mod.F90:125).
+    if (int rc = initial_diag(slot)) return rc;
+    *id = slot;
+    return GDC_OK;
+  }
+
+  int remove(int id) override {
+    if (!valid(id)) return fail(GDC_E_CONFIG, "remove: unknown member");
+    sync_stream();
+    MemberRec& r = recs[id];
+    cudaFree(r.dmem);
+    r = MemberRec();
+    std::memset(&hdesc[id], 0, sizeof(MemberDev<T>));
+    dirty = true;
+    return GDC_OK;
+  }
+
+  // --------------------------------------------------------------- steps
+  int step(int n) override {
+    for (int k = 0; k < n; ++k) {
+      if (dirty)
+        if (int rc = rebuild()) return rc;
+      if (nwork == 0) return GDC_OK;
+      int rc = GDC_OK;
+      const int par = old_ == SL_L1 ? 0 : 1;
+      if (use_graph && warm) {
+        if (!gexec[par]) rc = capture(par);
+        if (rc == GDC_OK && gexec[par]) {
+          cudaError_t e = cudaGraphLaunch(gexec[par], stream);
+          if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("cudaGraphLaunch", e));
+        } else if (rc == GDC_OK) {
+          rc = enqueue_step(nullptr);
+        }
+      } else {
+        rc = enqueue_step(nullptr);
+        warm = true;
+      }
+      if (rc) return rc;
+      advance_bookkeeping();
+    }
+    return GDC_OK;
+  }
+
+  // time_advance (src/time_mod.F90:106-130) plus host-side step accounting
+  // (deterministic, no device round trip).
+  void advance_bookkeeping() {
+    std::swap(old_, new_);
+    bool changed = false;
+    for (int s : active_slots) {
+      MemberRec& r = recs[s];
+      r.level = old_;
+      ++r.steps_done;
+      if (r.steps_done >= r.nsteps) {
+        r.active = false;
+        r.finished = true;
+        changed = true;
+      }
+    }
+    if (changed) dirty = true;
+  }
+
+  int sync() override {
+    cudaError_t e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("sync", e));
+    std::vector<long long> nan(kSlots);
+    e = cudaMemcpy(nan.data(), d_nan, sizeof(long long) * kSlots, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("sync: nan flags", e));
+    for (int s = 0; s < kSlots; ++s) {
+      MemberRec& r = recs[s];
+      if (!r.used || nan[s] < 0 || r.nan) continue;
+      // A member whose mass or energy became NaN is evicted from the batch
+      // (the reference stops the program, src/diag_mod.F90:79-87); the
+      // others continue.
+      r.nan = true;
+      r.nan_step = nan[s];
+      if (r.active) {
+        r.active = false;
+        r.finished = true;
+        dirty = true;
+      }
+    }
+    return GDC_OK;
+  }
+
+  int member_info(int id, long long* steps, int* fin, long long* nan) override {
+    if (!valid(id)) return fail(GDC_E_CONFIG, "member_info: unknown member");
+    const MemberRec& r = recs[id];
+    if (steps) *steps = r.steps_done;
+    if (fin) *fin = r.finished ? 1 : 0;
+    if (nan) *nan = r.nan_step;
+    return GDC_OK;
+  }
+
+  int active(int* n) override {
+    int c = 0;
+    for (auto& r : recs) c += (r.used && r.active) ? 1 : 0;
+    *n = c;
+    return GDC_OK;
+  }
+
+  int get_state(int id, double* u, double* v, double* gd, double* iu, double* iv, double* ig,
+                int ld) override {
+    if (!valid(id)) return fail(GDC_E_CONFIG, "get_state: unknown member");
+    const MemberRec& r = recs[id];
+    const int N = r.N, M = r.M, Mh = M - 1;
+    if (ld < N + 4) return fail(GDC_E_CONFIG, "get_state: ld < num_lon + 4");
+    sync_stream();
+    // state(old) of this member: its last written level.
+    const int lvl = level_of(id);
+    const MemberDev<T>& d = hdesc[id];
+    std::vector<double> hg, hu, hv;
+    cudaError_t e = download_field(d.st[lvl][F_GD], d.lo[lvl][F_GD], (size_t)M * N, hg);
+    if (e == cudaSuccess) e = download_field(d.st[lvl][F_IU], d.lo[lvl][F_IU], (size_t)M * N, hu);
+    if (e == cudaSuccess) e = download_field(d.st[lvl][F_IV], d.lo[lvl][F_IV], (size_t)Mh * N, hv);
+    if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("get_state", e));
+    std::vector<double> sg((size_t)M * N);
+    for (size_t q = 0; q < sg.size(); ++q) sg[q] = std::sqrt(hg[q]);
+    auto put = [&](double* f, int rows, auto value) {
+      if (!f) return;
+      std::memset(f, 0, sizeof(double) * (size_t)ld * (rows + 4));
+      for (int j = 0; j < rows; ++j)
+        for (int i = 0; i < N; ++i) f[(size_t)(j + 2) * ld + i + 2] = value(i, j);
+      for (int j = 0; j < rows + 4; ++j) {
+        double* row = f + (size_t)j * ld;
+        row[0] = row[N];
+        row[1] = row[N + 1];
+        row[N + 2] = row[2];
+        row[N + 3] = row[3];
+      }
+    };
+    put(gd, M, [&](int i, int j) { return hg[(size_t)j * N + i]; });
+    put(iu, M, [&](int i, int j) { return hu[(size_t)j * N + i]; });
+    put(iv, Mh, [&](int i, int j) { return hv[(size_t)j * N + i]; });
+    put(ig, M, [&](int i, int j) { return sg[(size_t)j * N + i]; });
+    if (r.steps_done == 0) {
+      // state(old) still holds the initial condition's own u and v.
+      auto copy_ic = [&](double* f, const std::vector<double>& src, int rows) {
+        if (!f) return;
+        for (int j = 0; j < rows + 4; ++j)
+          for (int i = 0; i < N + 4; ++i) f[(size_t)j * ld + i] = src[(size_t)j * r.ic_ld + i];
+      };
+      copy_ic(u, r.ic_u, M);
+      copy_ic(v, r.ic_v, Mh);
+    } else {
+      // update_state's recovery of u and v (src/dycore_mod.F90:636-645).
+      put(u, M, [&](int i, int j) {
+        if (j == 0 || j == M - 1) return 0.0;
+        const int ip = (i + 1) % N;
+        return hu[(size_t)j * N + i] * 2.0 / (sg[(size_t)j * N + i] + sg[(size_t)j * N + ip]);
+      });
+      put(v, Mh, [&](int i, int j) {
+        return hv[(size_t)j * N + i] * 2.0 / (sg[(size_t)j * N + i] + sg[(size_t)(j + 1) * N + i]);
+      });
+    }
+    return GDC_OK;
+  }
+
+  int diag(int id, double* m, double* e, double* b) override {
+    if (!valid(id)) return fail(GDC_E_CONFIG, "diag: unknown member");
+    sync_stream();
+    double h[3];
+    cudaError_t er = cudaMemcpy(h, d_diag + 3 * id, sizeof(h), cudaMemcpyDeviceToHost);
+    if (er != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("diag", er));
+    if (m) *m = h[0];
+    if (e) *e = h[1];
+    if (b) *b = h[2];
+    return GDC_OK;
+  }
+
+  int set_tile(int r, int c) override {
+    if (r == 0 && c == 0) {
+      r = 8;
+      c = 32;
+    }
+    if (r < 1 || r > 32 || c < 8 || c > 256 || r * c > 4096)
+      return fail(GDC_E_CONFIG, "set_tile: rows in 1..32, cols in 8..256, rows*cols <= 4096");
+    tile_r = r;
+    tile_c = c;
+    dirty = true;
+    return GDC_OK;
+  }
+
+  int set_stream(void* s) override {
+    sync_stream();
+    stream = s ? (cudaStream_t)s : own_stream;
+    invalidate_graphs();
+    return GDC_OK;
+  }
+
+  // Times each candidate tile shape on the current members (graph replay,
+  // CUDA events) and keeps the fastest.  Advances the members.
+  int autotune(int* rr, int* cc, double* best_ms) override {
+    static const int cand[][2] = {{4, 32}, {8, 32}, {16, 32}, {4, 64}, {8, 64}, {2, 128}, {4, 128}, {16, 16}};
+    double best = 1e30;
+    int br = tile_r, bc = tile_c;
+    for (auto& c : cand) {
+      if (int rc = set_tile(c[0], c[1])) return rc;
+      if (int rc = step(1)) return rc;  // build + warm
+      if (nwork == 0) break;
+      cudaEvent_t e0, e1;
+      cudaEventCreate(&e0);
+      cudaEventCreate(&e1);
+      const int reps = 3;
+      if (int rc = step(1)) return rc;
+      cudaEventRecord(e0, stream);
+      if (int rc = step(reps)) return rc;
+      cudaEventRecord(e1, stream);
+      cudaEventSynchronize(e1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      if (ms / reps < best) {
+        best = ms / reps;
+        br = c[0];
+        bc = c[1];
+      }
+    }
+    set_tile(br, bc);
+    if (rr) *rr = br;
+    if (cc) *cc = bc;
+    if (best_ms) *best_ms = best;
+    return GDC_OK;
+  }
+
+  int profile(int n, double* ms, long long* launches) override {
+    for (int k = 0; k < 4; ++k) {
+      ms[k] = 0;
+      launches[k] = 0;
+    }
+    for (int s = 0; s < n; ++s) {
+      if (dirty)
+        if (int rc = rebuild()) return rc;
+      if (nwork == 0) break;
+      prof.clear();
+      if (int rc = enqueue_step(&prof)) return rc;
+      cudaError_t e = cudaStreamSynchronize(stream);
+      if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("profile", e));
+      for (auto& p : prof) {
+        float t = 0;
+        cudaEventElapsedTime(&t, p.e0, p.e1);
+        ms[p.kind] += t;
+        launches[p.kind] += 1;
+        cudaEventDestroy(p.e0);
+        cudaEventDestroy(p.e1);
+      }
+      prof.clear();
+      advance_bookkeeping();
+    }
+    return GDC_OK;
+  }
+
+  int debug_tendency(int id, int pass, double* du, double* dv, double* dgd, int ld) override {
+    if (!valid(id)) return fail(GDC_E_CONFIG, "debug_tendency: unknown member");
+    if (pass < 0 || pass > 2) return fail(GDC_E_CONFIG, "debug_tendency: pass must be 0, 1 or 2");
+    const MemberRec& r = recs[id];
+    const int N = r.N, M = r.M, Mh = M - 1;
+    if (ld < N + 4) return fail(GDC_E_CONFIG, "debug_tendency: ld < num_lon + 4");
+    if (dirty)
+      if (int rc = rebuild()) return rc;
+    // One member's work items only.
+    std::vector<WorkItem> wl;
+    for (int q = 0; q < nwork; ++q)
+      if (hwl[q].member == id) wl.push_back(hwl[q]);
+    if (wl.empty()) {
+      // A finished member is not in the work list; build its items.
+      std::vector<WorkItem> all;
+      int pc = 0;
+      append_items(id, all, pc);
+      wl = all;
+    }
+    WorkItem* dwl = nullptr;
+    if (cudaMalloc(&dwl, sizeof(WorkItem) * wl.size()) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(GDC_E_OOM, "debug_tendency: cudaMalloc");
+    }
+    sync_stream();
+    cudaMemcpy(dwl, wl.data(), sizeof(WorkItem) * wl.size(), cudaMemcpyHostToDevice);
+    StageArgs a = base_args(pass);
+    a.in_slot = level_of(id);
+    a.tout = TS_NEW;
+    int rc = launch_stage<T>(d_mem, dwl, (int)wl.size(), P.uv_adv_scheme, tile_r, tile_c,
+                             std::max(max_n, N), a, stream);
+    cudaError_t e = cudaStreamSynchronize(stream);
+    cudaFree(dwl);
+    if (rc) return fail(rc, "debug_tendency: launch failed");
+    if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("debug_tendency", e));
+    const MemberDev<T>& d = hdesc[id];
+    std::vector<double> hg, hu, hv;
+    e = download_field(d.td[TS_NEW][F_GD], nullptr, (size_t)M * N, hg);
+    if (e == cudaSuccess) e = download_field(d.td[TS_NEW][F_IU], nullptr, (size_t)M * N, hu);
+    if (e == cudaSuccess) e = download_field(d.td[TS_NEW][F_IV], nullptr, (size_t)Mh * N, hv);
+    if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("debug_tendency: download", e));
+    auto put = [&](double* f, int rows, const std::vector<double>& src) {
+      if (!f) return;
+      std::memset(f, 0, sizeof(double) * (size_t)ld * (rows + 4));
+      for (int j = 0; j < rows; ++j)
+        for (int i = 0; i < N; ++i) f[(size_t)(j + 2) * ld + i + 2] = src[(size_t)j * N + i];
+    };
+    put(dgd, M, hg);
+    put(du, M, hu);
+    put(dv, Mh, hv);
+    return GDC_OK;
+  }
+
+ private:
+  struct Prof {
+    int kind;
+    cudaEvent_t e0, e1;
+  };
+
+  gdc_params P;
+  cudaStream_t own_stream = nullptr, stream = nullptr;
+  MemberDev<T>* d_mem = nullptr;
+  unsigned* d_counters = nullptr;
+  double* d_beta = nullptr;
+  double* d_diag = nullptr;
+  long long* d_steps = nullptr;
+  long long* d_nan = nullptr;
+  WorkItem* d_wl = nullptr;
+  size_t wl_cap = 0;
+  double* d_partials = nullptr;
+  size_t part_cap = 0;
+  std::vector<MemberRec> recs;
+  std::vector<MemberDev<T>> hdesc;
+  std::vector<WorkItem> hwl;
+  std::vector<int> active_slots;
+  int nwork = 0, max_n = 0;
+  int tile_r = 8, tile_c = 32;
+  int old_ = SL_L1, new_ = SL_L2;  // src/time_mod.F90:68-69
+  bool dirty = true, warm = false, use_graph = true;
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  std::vector<Prof> prof;
+  std::vector<void*> allocs;
+
+  int fail(int code, const std::string& m) {
+    err = m;
+    return code;
+  }
+  bool valid(int id) const { return id >= 0 && id < kSlots && recs[id].used; }
+  // The slot holding state(old) of a member (frozen once it finishes).
+  int level_of(int id) const { return recs[id].level; }
+
+  int dalloc(void** p, size_t n) {
+    cudaError_t e = cudaMalloc(p, n);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(GDC_E_OOM, cuda_msg("cudaMalloc", e));
+    }
+    allocs.push_back(*p);
+    return GDC_OK;
+  }
+
+  void sync_stream() {
+    if (stream) cudaStreamSynchronize(stream);
+  }
+
+  void invalidate_graphs() {
+    for (auto& g : gexec)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
+    warm = false;
+  }
+
+  void release() {
+    if (stream) cudaStreamSynchronize(stream);
+    invalidate_graphs();
+    for (auto& r : recs)
+      if (r.dmem) cudaFree(r.dmem);
+    for (void* p : allocs) cudaFree(p);
+    if (d_wl) cudaFree(d_wl);
+    if (d_partials) cudaFree(d_partials);
+    if (own_stream) cudaStreamDestroy(own_stream);
+  }
+
+  cudaError_t upload_field(T* dst, T* lo, const std::vector<double>& src) {
+    std::vector<T> hi(src.size()), lw;
+    if (lo) lw.resize(src.size());
+    for (size_t q = 0; q < src.size(); ++q) {
+      hi[q] = T(src[q]);
+      if (lo) lw[q] = T(src[q] - (double)hi[q]);
+    }
+    cudaError_t e = cudaMemcpy(dst, hi.data(), hi.size() * sizeof(T), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && lo) e = cudaMemcpy(lo, lw.data(), lw.size() * sizeof(T), cudaMemcpyHostToDevice);
+    return e;
+  }
+
+  cudaError_t download_field(const T* src, const T* lo, size_t n, std::vector<double>& out) {
+    std::vector<T> hi(n), lw;
+    cudaError_t e = cudaMemcpy(hi.data(), src, n * sizeof(T), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && lo) {
+      lw.resize(n);
+      e = cudaMemcpy(lw.data(), lo, n * sizeof(T), cudaMemcpyDeviceToHost);
+    }
+    out.resize(n);
+    for (size_t q = 0; q < n; ++q) out[q] = (double)hi[q] + (lo ? (double)lw[q] : 0.0);
+    return e;
+  }
+
+  void append_items(int s, std::vector<WorkItem>& out, int& pcount) {
+    const MemberRec& r = recs[s];
+    const int N = r.N, M = r.M;
+    int pbase = pcount;
+    // Whole-row tasks first (they are the longest items).
+    for (int j = 0; j < M; ++j)
+      if (r.rowinfo[j] & RI_SPECIAL) out.push_back(WorkItem{s, 1, j, 0, 1, N, pcount++, 0});
+    // Bulk tiles over runs of ordinary rows.
+    int j = 0;
+    while (j < M) {
+      if (r.rowinfo[j] & RI_SPECIAL) {
+        ++j;
+        continue;
+      }
+      int b = j;
+      while (b + 1 < M && !(r.rowinfo[b + 1] & RI_SPECIAL)) ++b;
+      for (int j0 = j; j0 <= b; j0 += tile_r) {
+        const int rows = std::min(tile_r, b - j0 + 1);
+        for (int i0 = 0; i0 < N; i0 += tile_c)
+          out.push_back(WorkItem{s, 0, j0, i0, rows, std::min(tile_c, N - i0), pcount++, 0});
+      }
+      j = b + 1;
+    }
+    hdesc[s].pbase = pbase;
+    hdesc[s].pcount = pcount - pbase;
+  }
+
+  int rebuild() {
+    sync_stream();
+    invalidate_graphs();
+    active_slots.clear();
+    std::vector<WorkItem> rows_first, tiles;
+    int pc = 0;
+    max_n = 8;
+    for (int s = 0; s < kSlots; ++s) {
+      if (!recs[s].used || !recs[s].active) continue;
+      active_slots.push_back(s);
+      std::vector<WorkItem> items;
+      append_items(s, items, pc);
+      for (auto& w : items) (w.kind ? rows_first : tiles).push_back(w);
+      max_n = std::max(max_n, recs[s].N);
+    }
+    hwl = rows_first;
+    hwl.insert(hwl.end(), tiles.begin(), tiles.end());
+    nwork = (int)hwl.size();
+    if ((size_t)nwork > wl_cap) {
+      if (d_wl) cudaFree(d_wl);
+      d_wl = nullptr;
+      wl_cap = std::max<size_t>(nwork, 2 * wl_cap);
+      cudaError_t e = cudaMalloc(&d_wl, wl_cap * sizeof(WorkItem));
+      if (e != cudaSuccess) return fail(GDC_E_OOM, cuda_msg("rebuild: work list", e));
+    }
+    if ((size_t)pc > part_cap) {
+      if (d_partials) cudaFree(d_partials);
+      d_partials = nullptr;
+      part_cap = std::max<size_t>(pc, 2 * part_cap);
+      cudaError_t e = cudaMalloc(&d_partials, part_cap * 2 * sizeof(double));
+      if (e != cudaSuccess) return fail(GDC_E_OOM, cuda_msg("rebuild: partials", e));
+    }
+    cudaError_t e = cudaSuccess;
+    if (nwork) e = cudaMemcpy(d_wl, hwl.data(), nwork * sizeof(WorkItem), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_mem, hdesc.data(), sizeof(MemberDev<T>) * kSlots, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("rebuild: upload", e));
+    dirty = false;
+    return GDC_OK;
+  }
+
+  StageArgs base_args(int pass) const {
+    StageArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.pass = pass;
+    a.in_slot = a.base_slot = a.out_slot = -1;
+    a.tout = a.tprev = a.tadd = a.tadd2 = a.taccum = -1;
+    a.tadd_sign = 1;
+    a.scale2 = 1.0;
+    a.h_scale = 0.5;
+    a.ip_slot = -1;
+    a.partials = d_partials;
+    a.counters = d_counters;
+    a.beta = d_beta;
+    a.qcon = P.qcon_modified;
+    a.ub_lon = P.uv_adv_upwind_lon_beta;
+    a.ub_lat = P.uv_adv_upwind_lat_beta;
+    a.rescale_rtol = P.filter_rescale_rtol;
+    return a;
+  }
+
+  // Launch wrappers with optional per-launch CUDA events (profile mode).
+  int run_stage(const StageArgs& a, std::vector<Prof>* pr) {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (pr) {
+      cudaEventCreate(&e0);
+      cudaEventCreate(&e1);
+      cudaEventRecord(e0, stream);
+    }
+    int rc = launch_stage<T>(d_mem, d_wl, nwork, P.uv_adv_scheme, tile_r, tile_c, max_n, a, stream);
+    if (pr) {
+      cudaEventRecord(e1, stream);
+      pr->push_back(Prof{0, e0, e1});
+    }
+    return rc ? fail(rc, "stage launch failed") : GDC_OK;
+  }
+  int run_final(const FinalArgs& a, std::vector<Prof>* pr) {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (pr) {
+      cudaEventCreate(&e0);
+      cudaEventCreate(&e1);
+      cudaEventRecord(e0, stream);
+    }
+    int rc = launch_final<T>(d_mem, d_wl, nwork, a, stream);
+    if (pr) {
+      cudaEventRecord(e1, stream);
+      pr->push_back(Prof{1, e0, e1});
+    }
+    return rc ? fail(rc, "final-update launch failed") : GDC_OK;
+  }
+
+  // One predict_correct call (src/dycore_mod.F90:754-792) from level o to n.
+  int predict_correct(int pass, int o, int n, std::vector<Prof>* pr) {
+    StageArgs a = base_args(pass);
+    a.in_slot = o;
+    a.base_slot = o;
+    a.out_slot = SL_SA;
+    if (int rc = run_stage(a, pr)) return rc;  // predict 1
+    a = base_args(pass);
+    a.in_slot = SL_SA;
+    a.base_slot = o;
+    a.out_slot = SL_SB;
+    a.tout = TS_OLD;
+    if (int rc = run_stage(a, pr)) return rc;  // predict 2
+    a = base_args(pass);
+    a.in_slot = SL_SB;
+    a.tout = TS_NEW;
+    a.tprev = TS_OLD;
+    a.do_ip = 1;
+    if (int rc = run_stage(a, pr)) return rc;  // correct + beta
+    FinalArgs f;
+    f.base_slot = o;
+    f.out_slot = n;
+    f.tslot = TS_NEW;
+    f.pass = pass;
+    f.use_lo = sizeof(T) == 4 ? 1 : 0;
+    f.h_scale = 1.0;
+    f.beta = d_beta;
+    return run_final(f, pr);
+  }
+
+  // isp_splitting (src/dycore_mod.F90:689-752).
+  int isp(std::vector<Prof>* pr) {
+    const int m = P.subcycles;
+    if (int rc = launch_copy_state<T>(d_mem, d_wl, nwork, old_, SL_SAVED, stream))
+      return fail(rc, "copy launch failed");
+    StageArgs a = base_args(kSlowPass);
+    a.in_slot = old_;
+    a.tout = TS_SLOW;
+    if (int rc = run_stage(a, pr)) return rc;
+    int t1 = old_, t2 = SL_L0;
+    for (int k = 1; k <= m; ++k) {
+      a = base_args(kFastPass);
+      a.in_slot = t1;
+      a.base_slot = t1;
+      a.out_slot = SL_SA;
+      a.tadd = TS_SLOW;
+      if (int rc = run_stage(a, pr)) return rc;
+      a.in_slot = SL_SA;
+      a.out_slot = SL_SB;
+      if (int rc = run_stage(a, pr)) return rc;
+      a.in_slot = SL_SB;
+      a.out_slot = t2;
+      a.taccum = TS_ACCUM;
+      a.accum_init = k == 1;
+      a.h_scale = 1.0;
+      if (int rc = run_stage(a, pr)) return rc;
+      std::swap(t1, t2);
+    }
+    a = base_args(kSlowPass);
+    a.in_slot = t1;
+    a.base_slot = t1;
+    a.out_slot = SL_SA;
+    a.tadd = TS_SLOW;
+    a.tadd_sign = -1;
+    a.h_scale = 1.0;  // half_dt = pcdt[slow]
+    if (int rc = run_stage(a, pr)) return rc;
+    a.in_slot = SL_SA;
+    a.out_slot = SL_SB;
+    if (int rc = run_stage(a, pr)) return rc;
+    a = base_args(kSlowPass);
+    a.in_slot = SL_SB;
+    a.tout = TS_NEW;
+    a.tadd = TS_SLOW;
+    a.tadd2 = TS_ACCUM;
+    a.scale2 = 2.0 / m;
+    a.do_ip = 1;
+    a.beta_mode = 1;
+    a.ip_slot = SL_SAVED;
+    if (int rc = run_stage(a, pr)) return rc;
+    FinalArgs f;
+    f.base_slot = SL_SAVED;
+    f.out_slot = new_;
+    f.tslot = TS_NEW;
+    f.pass = kAllPass;
+    f.use_lo = sizeof(T) == 4 ? 1 : 0;
+    f.h_scale = 0.5;
+    f.beta = d_beta;
+    return run_final(f, pr);
+  }
+
+  int enqueue_step(std::vector<Prof>* pr) {
+    int rc = GDC_OK;
+    if (P.split_scheme == GDC_SPLIT_CSP2) {
+      // csp2_splitting (src/dycore_mod.F90:671-687)
+      int t1 = SL_L0, t2 = old_;
+      rc = predict_correct(kSlowPass, old_, t1, pr);
+      for (int k = 0; k < P.subcycles && !rc; ++k) {
+        rc = predict_correct(kFastPass, t1, t2, pr);
+        std::swap(t1, t2);
+      }
+      if (!rc) rc = predict_correct(kSlowPass, t1, new_, pr);
+    } else if (P.split_scheme == GDC_SPLIT_ISP) {
+      rc = isp(pr);
+    } else {
+      rc = predict_correct(kAllPass, old_, new_, pr);
+    }
+    if (rc) return rc;
+    if (P.use_diffusion) {
+      // ordinary_diffusion(time_step_size, state(new)), order 2, sign +1.
+      const double c = 1.0 * P.time_step_size * P.diffusion_coef;
+      cudaEvent_t e0 = nullptr, e1 = nullptr;
+      if (pr) {
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, stream);
+      }
+      rc = launch_diffusion<T>(d_mem, d_wl, nwork, tile_r, tile_c, max_n, new_, c, stream);
+      if (pr) {
+        cudaEventRecord(e1, stream);
+        pr->push_back(Prof{3, e0, e1});
+      }
+      if (rc) return fail(rc, "diffusion launch failed");
+    }
+    // diag_run(state(old)) after time_advance (src/dycore_mod.F90:135).
+    DiagArgs d;
+    d.slot = new_;
+    d.partials = d_partials;
+    d.counters = d_counters;
+    d.diag = d_diag;
+    d.beta = d_beta;
+    d.steps = d_steps;
+    d.nan_step = d_nan;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (pr) {
+      cudaEventCreate(&e0);
+      cudaEventCreate(&e1);
+      cudaEventRecord(e0, stream);
+    }
+    rc = launch_diag<T>(d_mem, d_wl, nwork, d, stream);
+    if (pr) {
+      cudaEventRecord(e1, stream);
+      pr->push_back(Prof{2, e0, e1});
+    }
+    return rc ? fail(rc, "diag launch failed") : GDC_OK;
+  }
+
+  // diag_run of a freshly admitted member's initial state.
+  int initial_diag(int slot) {
+    std::vector<WorkItem> wl;
+    int pc = 0;
+    const MemberDev<T> saved = hdesc[slot];
+    append_items(slot, wl, pc);
+    WorkItem* dwl = nullptr;
+    double* dpart = nullptr;
+    if (cudaMalloc(&dwl, sizeof(WorkItem) * wl.size()) != cudaSuccess ||
+        cudaMalloc(&dpart, sizeof(double) * 2 * wl.size()) != cudaSuccess) {
+      cudaGetLastError();
+      if (dwl) cudaFree(dwl);
+      return fail(GDC_E_OOM, "initial diag: cudaMalloc");
+    }
+    cudaMemcpy(dwl, wl.data(), sizeof(WorkItem) * wl.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(d_mem + slot, &hdesc[slot], sizeof(MemberDev<T>), cudaMemcpyHostToDevice);
+    DiagArgs d;
+    d.slot = old_;
+    d.partials = dpart;
+    d.counters = d_counters;
+    d.diag = d_diag;
+    d.beta = nullptr;
+    d.steps = d_steps;
+    d.nan_step = d_nan;
+    int rc = launch_diag<T>(d_mem, dwl, (int)wl.size(), d, stream);
+    cudaError_t e = cudaStreamSynchronize(stream);
+    // The initial diag is not a step: reset the step counter.
+    const long long zero = 0;
+    cudaMemcpy(d_steps + slot, &zero, sizeof(zero), cudaMemcpyHostToDevice);
+    cudaFree(dwl);
+    cudaFree(dpart);
+    hdesc[slot].pbase = saved.pbase;
+    hdesc[slot].pcount = saved.pcount;
+    if (rc || e != cudaSuccess) return fail(GDC_E_CUDA, "initial diag failed");
+    return GDC_OK;
+  }
+
+  int capture(int par) {
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+      use_graph = false;
+      return GDC_OK;
+    }
+    int rc = enqueue_step(nullptr);
+    e = cudaStreamEndCapture(stream, &g);
+    if (rc || e != cudaSuccess || !g) {
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      use_graph = false;
+      return rc;
+    }
+    e = cudaGraphInstantiate(&gexec[par], g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      gexec[par] = nullptr;
+      use_graph = false;
+    }
+    return GDC_OK;
+  }
+};
+
+}  // namespace gdc
+
+// ------------------------------------------------------------------ C ABI
+
+struct gdc_batch {
+  std::unique_ptr<gdc::BatchIface> impl;
+  gdc_params p;
+  std::string err;
+};
+
+struct gdc_handle {
+  gdc_batch* b = nullptr;
+  int id = -1;
+  gdc_params p;
+  std::string err;
+};
+
+namespace {
+
+int validate_scheme(const gdc_params* p, std::string& err) {
+  if (!p) {
+    err = "null params";
+    return GDC_E_CONFIG;
+  }
+  if (p->uv_adv_scheme == GDC_ADV_WENO) {
+    err = "uv_adv_scheme 'weno' is not supported";
+    return GDC_E_CONFIG;
+  }
+  if (p->uv_adv_scheme != GDC_ADV_CENTER_DIFF && p->uv_adv_scheme != GDC_ADV_UPWIND) {
+    err = "Unknown uv_adv_scheme";
+    return GDC_E_CONFIG;
+  }
+  if (p->split_scheme < 0 || p->split_scheme > 3) {
+    err = "Unknown split_scheme";
+    return GDC_E_CONFIG;
+  }
+  if ((p->split_scheme == GDC_SPLIT_CSP2 || p->split_scheme == GDC_SPLIT_ISP) && p->subcycles < 1) {
+    err = "subcycles must be >= 1";
+    return GDC_E_CONFIG;
+  }
+  if (p->use_diffusion && p->diffusion_order != 2) {
+    err = "only diffusion_order = 2 is supported";
+    return GDC_E_CONFIG;
+  }
+  if (!(p->filter_rescale_rtol >= 0.0)) {
+    err = "filter_rescale_rtol must be >= 0";
+    return GDC_E_CONFIG;
+  }
+  if (p->precision != GDC_FP64 && p->precision != GDC_FP32) {
+    err = "precision must be GDC_FP64 or GDC_FP32";
+    return GDC_E_CONFIG;
+  }
+  return GDC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gdc_batch_create(const gdc_params* scheme, gdc_batch** out) {
+  if (!out) return GDC_E_CONFIG;
+  *out = nullptr;
+  std::string err;
+  if (int rc = validate_scheme(scheme, err)) {
+    std::fprintf(stderr, "gdc_batch_create: %s\n", err.c_str());
+    return rc;
+  }
+  auto* b = new gdc_batch();
+  b->p = *scheme;
+  int rc;
+  if (scheme->precision == GDC_FP32) {
+    auto* impl = new gdc::Batch<float>(*scheme);
+    b->impl.reset(impl);
+    rc = impl->init();
+  } else {
+    auto* impl = new gdc::Batch<double>(*scheme);
+    b->impl.reset(impl);
+    rc = impl->init();
+  }
+  if (rc) {
+    std::fprintf(stderr, "gdc_batch_create: %s\n", b->impl->err.c_str());
+    delete b;
+    return rc;
+  }
+  *out = b;
+  return GDC_OK;
+}
+
+void gdc_batch_destroy(gdc_batch* b) { delete b; }
+const char* gdc_batch_last_error(const gdc_batch* b) { return b ? b->impl->err.c_str() : "null batch"; }
+int gdc_batch_set_stream(gdc_batch* b, void* s) { return b ? b->impl->set_stream(s) : GDC_E_CONFIG; }
+
+size_t gdc_member_bytes(const gdc_params* scheme, int num_lon, int num_lat) {
+  return scheme ? gdc::member_bytes_for(*scheme, num_lon, num_lat) : 0;
+}
+
+int gdc_device_mem_info(int device, size_t* free_bytes, size_t* total_bytes) {
+  if (cudaSetDevice(device) != cudaSuccess) return GDC_E_CUDA;
+  size_t f = 0, t = 0;
+  if (cudaMemGetInfo(&f, &t) != cudaSuccess) return GDC_E_CUDA;
+  if (free_bytes) *free_bytes = f;
+  if (total_bytes) *total_bytes = t;
+  return GDC_OK;
+}
+
+int gdc_batch_add(gdc_batch* b, int num_lon, int num_lat, double time_step_size, long long nsteps,
+                  const int* cutoff, const double* u, const double* v, const double* gd,
+                  const double* ghs, int ld, size_t reserve_bytes, int* member_id) {
+  if (!b || !member_id) return GDC_E_CONFIG;
+  return b->impl->add(num_lon, num_lat, time_step_size, nsteps, cutoff, u, v, gd, ghs, ld,
+                      reserve_bytes, member_id);
+}
+int gdc_batch_remove(gdc_batch* b, int id) { return b ? b->impl->remove(id) : GDC_E_CONFIG; }
+int gdc_batch_step(gdc_batch* b, int nsteps) { return b ? b->impl->step(nsteps) : GDC_E_CONFIG; }
+int gdc_batch_sync(gdc_batch* b) { return b ? b->impl->sync() : GDC_E_CONFIG; }
+int gdc_batch_member_info(gdc_batch* b, int id, long long* steps, int* fin, long long* nan) {
+  return b ? b->impl->member_info(id, steps, fin, nan) : GDC_E_CONFIG;
+}
+int gdc_batch_get_state(gdc_batch* b, int id, double* u, double* v, double* gd, int ld) {
+  return b ? b->impl->get_state(id, u, v, gd, nullptr, nullptr, nullptr, ld) : GDC_E_CONFIG;
+}
+int gdc_batch_diag(gdc_batch* b, int id, double* m, double* e, double* beta) {
+  return b ? b->impl->diag(id, m, e, beta) : GDC_E_CONFIG;
+}
+int gdc_batch_active(gdc_batch* b, int* n) { return (b && n) ? b->impl->active(n) : GDC_E_CONFIG; }
+int gdc_batch_set_tile(gdc_batch* b, int r, int c) { return b ? b->impl->set_tile(r, c) : GDC_E_CONFIG; }
+int gdc_batch_autotune(gdc_batch* b, int* r, int* c, double* ms) {
+  return b ? b->impl->autotune(r, c, ms) : GDC_E_CONFIG;
+}
+int gdc_batch_profile(gdc_batch* b, int nsteps, double* ms, long long* launches) {
+  return (b && ms && launches) ? b->impl->profile(nsteps, ms, launches) : GDC_E_CONFIG;
+}
+
+double gdc_algorithmic_bytes_per_gpt_step(const gdc_params* p) {
+  if (!p) return 0;
+  // Prognostic words {gd, iap u, iap v} (+ ghs) read and written per
+  // predict_correct call: stage 1 reads 4 writes 3, stage 2 reads 7 writes
+  // 6, stage 3 reads 7 writes 3, the final update reads 6 writes 3: 39.
+  double calls = 1;
+  if (p->split_scheme == GDC_SPLIT_CSP2) calls = p->subcycles + 2;
+  double words = 39.0 * calls;
+  if (p->split_scheme == GDC_SPLIT_ISP) {
+    // copy 6, slow tendency 7, per subcycle 13 + 13 + 16, slow 13 + 13 + 13,
+    // final update 9.
+    words = 6 + 7 + p->subcycles * 42.0 + 39 + 9;
+  }
+  if (p->use_diffusion) words += 6;
+  const double wbytes = p->precision == GDC_FP32 ? 4.0 : 8.0;
+  return words * wbytes;
+}
+
+// ---- single model
+
+int gdc_create(const gdc_params* p, gdc_handle** out) {
+  if (!out) return GDC_E_CONFIG;
+  *out = nullptr;
+  std::string err;
+  if (int rc = validate_scheme(p, err)) {
+    std::fprintf(stderr, "gdc_create: %s\n", err.c_str());
+    return rc;
+  }
+  if (p->num_lon < 8 || p->num_lat < 5 || !(p->time_step_size > 0)) {
+    std::fprintf(stderr, "gdc_create: invalid num_lon, num_lat or time_step_size\n");
+    return GDC_E_CONFIG;
+  }
+  auto* h = new gdc_handle();
+  h->p = *p;
+  int rc = gdc_batch_create(p, &h->b);
+  if (rc) {
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return GDC_OK;
+}
+
+void gdc_destroy(gdc_handle* h) {
+  if (!h) return;
+  gdc_batch_destroy(h->b);
+  delete h;
+}
+
+const char* gdc_last_error(const gdc_handle* h) {
+  if (!h) return "null handle";
+  if (!h->err.empty()) return h->err.c_str();
+  return gdc_batch_last_error(h->b);
+}
+
+int gdc_set_state(gdc_handle* h, const double* u, const double* v, const double* gd,
+                  const double* ghs, int ld) {
+  if (!h) return GDC_E_CONFIG;
+  h->err.clear();
+  if (h->id >= 0) {
+    gdc_batch_remove(h->b, h->id);
+    h->id = -1;
+  }
+  // The single model runs until told otherwise: length is bounded by the
+  // caller's gdc_step calls, not by the member's nsteps.
+  return gdc_batch_add(h->b, h->p.num_lon, h->p.num_lat, h->p.time_step_size, (1LL << 62),
+                       nullptr, u, v, gd, ghs, ld, 0, &h->id);
+}
+
+int gdc_step(gdc_handle* h, int nsteps) {
+  if (!h) return GDC_E_CONFIG;
+  if (h->id < 0) {
+    h->err = "gdc_step before gdc_set_state";
+    return GDC_E_STATE;
+  }
+  if (nsteps < 0) return GDC_E_CONFIG;
+  return gdc_batch_step(h->b, nsteps);
+}
+
+int gdc_sync(gdc_handle* h) {
+  if (!h) return GDC_E_CONFIG;
+  int rc = gdc_batch_sync(h->b);
+  if (rc || h->id < 0) return rc;
+  long long nan = -1;
+  gdc_batch_member_info(h->b, h->id, nullptr, nullptr, &nan);
+  if (nan >= 0) {
+    h->err = "Total mass or energy is NaN at step " + std::to_string(nan) + "!";
+    return GDC_E_NAN;
+  }
+  return GDC_OK;
+}
+
+int gdc_run(gdc_handle* h, int nsteps) {
+  int rc = gdc_step(h, nsteps);
+  if (rc) return rc;
+  return gdc_sync(h);
+}
+
+int gdc_get_state(gdc_handle* h, double* u, double* v, double* gd, int ld) {
+  if (!h) return GDC_E_CONFIG;
+  if (h->id < 0) {
+    h->err = "gdc_get_state before gdc_set_state";
+    return GDC_E_STATE;
+  }
+  return h->b->impl->get_state(h->id, u, v, gd, nullptr, nullptr, nullptr, ld);
+}
+
+int gdc_get_iap(gdc_handle* h, double* iu, double* iv, double* ig, int ld) {
+  if (!h) return GDC_E_CONFIG;
+  if (h->id < 0) {
+    h->err = "gdc_get_iap before gdc_set_state";
+    return GDC_E_STATE;
+  }
+  return h->b->impl->get_state(h->id, nullptr, nullptr, nullptr, iu, iv, ig, ld);
+}
+
+int gdc_diag(gdc_handle* h, double* m, double* e, double* beta) {
+  if (!h) return GDC_E_CONFIG;
+  if (h->id < 0) {
+    h->err = "gdc_diag before gdc_set_state";
+    return GDC_E_STATE;
+  }
+  return h->b->impl->diag(h->id, m, e, beta);
+}
+
+int gdc_steps_done(gdc_handle* h, long long* steps) {
+  if (!h || !steps) return GDC_E_CONFIG;
+  if (h->id < 0) {
+    *steps = 0;
+    return GDC_OK;
+  }
+  return h->b->impl->member_info(h->id, steps, nullptr, nullptr);
+}
+
+int gdc_debug_tendency(gdc_handle* h, int pass, double* du, double* dv, double* dgd, int ld) {
+  if (!h) return GDC_E_CONFIG;
+  if (h->id < 0) {
+    h->err = "gdc_debug_tendency before gdc_set_state";
+    return GDC_E_STATE;
+  }
+  return h->b->impl->debug_tendency(h->id, pass, du, dv, dgd, ld);
+}
+
+int gdc_set_stream(gdc_handle* h, void* s) { return h ? gdc_batch_set_stream(h->b, s) : GDC_E_CONFIG; }
+
+}  // extern "C"

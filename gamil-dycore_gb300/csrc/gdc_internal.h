@@ -1,0 +1,188 @@
+// gdc_internal.h -- types shared by the host engine (gdc_engine.cpp,
+// gdc_host.cpp) and the CUDA kernels (gdc_kernels.cu).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <vector>
+
+#include "../../include/gdc.h"
+
+#ifdef __CUDACC__
+#define GDC_HD __host__ __device__
+#else
+#define GDC_HD
+#endif
+
+namespace gdc {
+
+// src/params_mod.F90:6-11 (FP64).
+constexpr double kPi = 3.141592653589793238462643383279502884;
+constexpr double kOmega = 2.0 * kPi / 86400.0;
+constexpr double kRadius = 6.37122e6;
+
+// ---------------------------------------------------------------- host mesh
+struct Mesh {
+  int N = 0, M = 0, Mh = 0;
+  double dlon = 0, dlat = 0;
+  std::vector<double> full_lat, half_lat, full_lon, half_lon;
+  std::vector<double> full_cos, half_cos, full_sin, half_sin;
+};
+struct Coef {
+  std::vector<double> full_cos, full_f, full_c, full_dlon, full_dlat;  // M
+  std::vector<double> half_cos, half_dlon, half_dlat;                  // Mh
+};
+Mesh make_mesh(int N, int M);
+Coef make_coef(const Mesh& m);
+void make_filter_rows(const Mesh& m, const gdc_params& p, std::vector<int>& flag_full,
+                      std::vector<int>& keep_full, std::vector<int>& flag_half,
+                      std::vector<int>& keep_half);
+
+// ------------------------------------------------------------ device layout
+// Passes of space_operators (src/dycore_mod.F90:34-36).
+enum Pass { kAllPass = 0, kFastPass = 1, kSlowPass = 2 };
+
+// Row coefficient table, per member, in the compute type.  Full-row tables
+// have M entries; half-row tables have Mh+2 entries with index 0 standing
+// for half row -1 and index Mh+1 for half row Mh (both 0.0: the reference
+// reads those out of bounds only to multiply a zero latitude halo).
+enum FullCoef {
+  CF_COS = 0,   // full_cos_lat after reset_cos_lat_at_poles
+  CF_F,         // 2 Omega sin
+  CF_C,         // sin / cos / a (0 at poles)
+  CF_RADVLON,   // 0.25 / full_dlon
+  CF_RADVLAT,   // 0.25 / full_dlat
+  CF_DLON,      // full_dlon
+  CF_DLAT,      // full_dlat
+  CF_C1,        // half_cos(j-1) / full_cos(j)
+  CF_C2,        // half_cos(j) / full_cos(j)
+  CF_MASSW,     // full_cos * dlon * dlat (diag total_mass weight)
+  CF_NFULL
+};
+enum HalfCoef {
+  CH_COS = 0,   // half_cos_lat
+  CH_RADVLON,   // 0.25 / half_dlon
+  CH_RADVLAT,   // 0.25 / half_dlat
+  CH_DLON,      // half_dlon
+  CH_DLAT,      // half_dlat
+  CH_NHALF
+};
+inline size_t coef_words(int M) { return (size_t)CF_NFULL * M + (size_t)CH_NHALF * (M + 1); }
+// Offset of table k: full tables first, then half tables (Mh+2 = M+1 each).
+GDC_HD inline size_t cf_off(int k, int M) { return (size_t)k * M; }
+GDC_HD inline size_t ch_off(int k, int M) { return (size_t)CF_NFULL * M + (size_t)k * (M + 1); }
+
+// Row information bits (per row index j = 0..M-1).
+enum RowBits {
+  RI_SPECIAL = 1,    // handled by a whole-row task (pole or filtered row)
+  RI_FLAG_FULL = 2,  // full row j is filtered
+  RI_FLAG_HALF = 4,  // half row j is filtered
+};
+// rowinfo[j] = bits | keep_full << 8 | keep_half << 20 (packed-coefficient
+// counts kept by the factor rows, 0..2046).
+GDC_HD inline int ri_keep_full(int r) { return (r >> 8) & 0xfff; }
+GDC_HD inline int ri_keep_half(int r) { return (r >> 20) & 0x7ff; }
+
+// Buffer slots of a member: time levels 0,1,2 of the reference
+// (state(0..2)), the isp saved state (state(-1)), and two stage states.
+enum Slot { SL_L0 = 0, SL_L1, SL_L2, SL_SAVED, SL_SA, SL_SB, SL_N };
+// Tendency slots (du, dv, dgd each).
+enum TSlot { TS_OLD = 0, TS_NEW, TS_SLOW, TS_ACCUM, TS_N };
+
+template <typename T>
+struct MemberDev {
+  int N, M, Mh;
+  int pbase, pcount;      // partial-sum slots of this member's work items
+  int pad0;
+  double pcdt[3];         // predict_correct time_step_size per Pass
+  double dt;              // time_step_size
+  T* st[SL_N][3];         // state slots: gd, iap u, iap v
+  T* lo[SL_N][3];         // compensation words (FP32 time levels), else null
+  T* td[TS_N][3];         // tendency slots: dgd, du, dv
+  T* ghs;
+  const T* coef;
+  const T* twid;          // cos(2 pi m/N), m<N, then sin(2 pi m/N)
+  const int* rowinfo;
+  const double* dcoef;    // FP64 diag weights: mass weight [M], full cos [M], half cos [Mh]
+};
+
+enum Field { F_GD = 0, F_IU = 1, F_IV = 2 };
+
+struct WorkItem {
+  int member;  // member slot
+  int kind;    // 0 bulk tile, 1 whole-row task
+  int j0;      // first row index (row task: the row)
+  int i0;      // first column (tile)
+  int rows;    // tile rows
+  int cols;    // tile columns
+  int pidx;    // partial-sum slot
+  int pad;
+};
+
+// What a stage launch does with the tendency T = space_operators(in):
+//   T' = T (+/- T_add) (+ scale2 * T_add2)           combine
+//   accum = (init ? 0 : accum) + T                    (isp fast sum)
+//   T_out = T'; S_out = base + h T'                   store / update
+//   partials of <P, T'> and <T', T'> with P = T_prev (beta_mode 0) or the
+//   state slot `ip_slot` (beta_mode 1), and the member's beta.
+struct StageArgs {
+  int pass;
+  int in_slot, base_slot, out_slot;  // Slot values (-1 unused)
+  int tout, tprev;                   // TSlot values (-1 unused)
+  int tadd, tadd_sign;               // TSlot added (+1) or subtracted (-1)
+  int tadd2;                         // TSlot added after scaling by scale2
+  double scale2;
+  int taccum, accum_init;            // TSlot accumulating T (pre-combine)
+  double h_scale;                    // update step = pcdt[pass] * h_scale
+  int do_ip;                         // form partials and beta
+  int beta_mode;                     // 0 predict_correct, 1 isp
+  int ip_slot;                       // state slot for beta_mode 1
+  double* partials;                  // 2 doubles per partial slot
+  unsigned* counters;                // per member, last-block detection
+  double* beta;                      // per member
+  int qcon;
+  double ub_lon, ub_lat;             // uv_adv_upwind_{lon,lat}_beta
+  double rescale_rtol;               // gdc_params::filter_rescale_rtol
+};
+
+struct FinalArgs {
+  int base_slot, out_slot, tslot;
+  int pass;
+  int use_lo;          // write compensated result (time level)
+  double h_scale;      // step = pcdt[pass] * h_scale * beta (or * 1)
+  const double* beta;  // per member or null
+};
+
+struct DiagArgs {
+  int slot;
+  double* partials;      // 2 doubles per partial slot
+  unsigned* counters;
+  double* diag;          // per member: mass, energy, beta
+  const double* beta;
+  long long* steps;      // per member: steps completed (incremented here)
+  long long* nan_step;   // per member: first step with NaN mass/energy
+};
+
+// Kernel launchers (gdc_kernels.cu).  `smem_limit` is the opt-in maximum.
+template <typename T>
+int launch_stage(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int adv, int tile_rows,
+                 int tile_cols, int max_n, const StageArgs& a, void* stream);
+template <typename T>
+int launch_final(const MemberDev<T>* mem, const WorkItem* wl, int nwork, const FinalArgs& a,
+                 void* stream);
+template <typename T>
+int launch_diag(const MemberDev<T>* mem, const WorkItem* wl, int nwork, const DiagArgs& a,
+                void* stream);
+// ordinary_diffusion (order 2): Laplacians of state `slot` into SA as
+// (gd', u', v'), then iap_transform of SA back into `slot`.
+template <typename T>
+int launch_diffusion(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int tile_rows,
+                     int tile_cols, int max_n, int slot, double sign_dt_coef, void* stream);
+template <typename T>
+int launch_copy_state(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int from_slot,
+                      int to_slot, void* stream);
+// Shared-memory bytes of one stage launch.
+template <typename T>
+size_t stage_smem_bytes(int tile_rows, int tile_cols, int max_n, int* staging_words);
+
+}  // namespace gdc

@@ -1,0 +1,18 @@
+// FP64 instantiation of the stage, update, diagnostic and diffusion kernels.
+// Compiled with --fmad=false: every point-wise FP64 expression is then
+// evaluated with the reference's own operations and rounding (no fused
+// multiply-add), so the plain path differs from the reference's arithmetic
+// only in the order of its parallel sums.
+#include "gdc_kernels.cuh"
+
+namespace gdc {
+
+template size_t stage_smem_bytes<double>(int, int, int, int*);
+template int launch_diffusion<double>(const MemberDev<double>*, const WorkItem*, int, int, int, int, int, double, void*);
+template int launch_copy_state<double>(const MemberDev<double>*, const WorkItem*, int, int, int, void*);
+template int launch_stage<double>(const MemberDev<double>*, const WorkItem*, int, int, int, int, int,
+                                  const StageArgs&, void*);
+template int launch_final<double>(const MemberDev<double>*, const WorkItem*, int, const FinalArgs&, void*);
+template int launch_diag<double>(const MemberDev<double>*, const WorkItem*, int, const DiagArgs&, void*);
+
+}  // namespace gdc

@@ -1,0 +1,133 @@
+"""ctypes wrapper of the CPU oracle (test infrastructure only).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs use
+this module, as the checker; the product never imports it.  Arrays use the
+reference's padded layout, numpy shape (rows + 4, num_lon + 4).
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+_P = ctypes.POINTER(ctypes.c_double)
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = ctypes.CDLL(str(path))
+        vp, dp, i = ctypes.c_void_p, _P, ctypes.c_int
+        ip = ctypes.POINTER(ctypes.c_int)
+        L.gdo_create.restype = vp
+        L.gdo_create.argtypes = [i, i, ctypes.c_double, i, i, i, i, ctypes.c_double, ctypes.c_double, i, ip, i,
+                                 ctypes.c_double, i]
+        L.gdo_destroy.argtypes = [vp]
+        L.gdo_set_rescale_rtol.argtypes = [vp, ctypes.c_double]
+        L.gdo_set_state.argtypes = [vp, dp, dp, dp, dp]
+        L.gdo_run_init.argtypes = [vp]
+        L.gdo_step.argtypes = [vp, i]
+        L.gdo_step.restype = i
+        L.gdo_get_state.argtypes = [vp, dp, dp, dp, dp, dp, dp]
+        L.gdo_diag.argtypes = [vp, dp, dp, dp]
+        L.gdo_tendency.argtypes = [vp, i, dp, dp, dp]
+        L.gdo_antisymmetry.argtypes = [vp, dp]
+        L.gdo_filter_row.argtypes = [vp, i, i, dp]
+        L.gdo_filter_flags.argtypes = [vp, ip, ip, ip, ip]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_P)
+
+
+def _pad(rows, N):
+    return np.zeros((rows + 4, N + 4))
+
+
+class OracleModel:
+    """The reference's dycore_init/run on the CPU, FP64, one thread."""
+
+    def __init__(self, num_lon, num_lat, time_step_size, subcycles=4, split_scheme=0, qcon_modified=1,
+                 uv_adv_scheme=0, upwind_lon_beta=0.0, upwind_lat_beta=0.5, use_zonal_tend_filter=1,
+                 cutoff=(), use_diffusion=0, diffusion_coef=0.0, diffusion_order=2, rescale_rtol=0.0):
+        self.N, self.M = num_lon, num_lat
+        c = (ctypes.c_int * 20)(*([0] * 20))
+        for k, x in enumerate(cutoff):
+            c[k] = int(x)
+        self.h = lib().gdo_create(num_lon, num_lat, time_step_size, subcycles, split_scheme, qcon_modified,
+                                  uv_adv_scheme, upwind_lon_beta, upwind_lat_beta, use_zonal_tend_filter, c,
+                                  use_diffusion, diffusion_coef, diffusion_order)
+        if rescale_rtol:
+            lib().gdo_set_rescale_rtol(self.h, rescale_rtol)
+
+    @classmethod
+    def from_params(cls, p):
+        """Build from a gdc.Params (any object with the same attribute names)."""
+        return cls(p.num_lon, p.num_lat, p.time_step_size, p.subcycles, p.split_scheme, p.qcon_modified,
+                   p.uv_adv_scheme, p.uv_adv_upwind_lon_beta, p.uv_adv_upwind_lat_beta, p.use_zonal_tend_filter,
+                   list(p.zonal_tend_filter_cutoff_wavenumber), p.use_diffusion, p.diffusion_coef,
+                   p.diffusion_order, getattr(p, "filter_rescale_rtol", 0.0))
+
+    def set_state(self, u, v, gd, ghs):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (u, v, gd, ghs)]
+        lib().gdo_set_state(self.h, *map(_ptr, arrs))
+        lib().gdo_run_init(self.h)
+
+    def step(self, n=1):
+        return lib().gdo_step(self.h, n)
+
+    def get_state(self):
+        N, M = self.N, self.M
+        u, v, gd = _pad(M, N), _pad(M - 1, N), _pad(M, N)
+        iu, iv, ig = _pad(M, N), _pad(M - 1, N), _pad(M, N)
+        lib().gdo_get_state(self.h, _ptr(u), _ptr(v), _ptr(gd), _ptr(iu), _ptr(iv), _ptr(ig))
+        return dict(u=u, v=v, gd=gd, iu=iu, iv=iv, ig=ig)
+
+    def diag(self):
+        m, e, b = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        lib().gdo_diag(self.h, ctypes.byref(m), ctypes.byref(e), ctypes.byref(b))
+        return m.value, e.value, b.value
+
+    def tendency(self, pass_=0):
+        N, M = self.N, self.M
+        du, dv, dgd = _pad(M, N), _pad(M - 1, N), _pad(M, N)
+        lib().gdo_tendency(self.h, pass_, _ptr(du), _ptr(dv), _ptr(dgd))
+        return du, dv, dgd
+
+    def antisymmetry(self):
+        out = np.zeros(4)
+        lib().gdo_antisymmetry(self.h, _ptr(out))
+        return out
+
+    def filter_row(self, half, lat_idx, x):
+        x = np.ascontiguousarray(x, dtype=np.float64).copy()
+        lib().gdo_filter_row(self.h, int(half), int(lat_idx), _ptr(x))
+        return x
+
+    def filter_flags(self):
+        M = self.M
+        ff, fh = (ctypes.c_int * M)(), (ctypes.c_int * (M - 1))()
+        cf, ch = (ctypes.c_int * M)(), (ctypes.c_int * (M - 1))()
+        lib().gdo_filter_flags(self.h, ff, fh, cf, ch)
+        return list(ff), list(fh), list(cf), list(ch)
+
+    def close(self):
+        if self.h:
+            lib().gdo_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,137 @@
+"""Oracle self-checks (CPU): the restatement against known answers.
+
+The reference ships no golden vectors and cannot be built here, so the
+oracle is pinned by identities the reference's own code implies:
+FFTPACK 5.1's coefficient packing (checked against numpy's FFT), the
+filter's row sets and kept modes, exact mass conservation with the filter
+off, and the antisymmetry identities of check_antisymmetry
+(src/dycore_mod.F90:794-851).
+"""
+import numpy as np
+import pytest
+
+from helpers import interior
+from oracle.oracle import OracleModel
+
+
+def fftpack_projection(x, c):
+    """FFTPACK rfft1f -> keep packed indices 1..2(c+1) -> rfft1b, via numpy."""
+    N = len(x)
+    X = np.fft.rfft(x)
+    Y = np.zeros_like(X)
+    Y[: c + 1] = X[: c + 1]
+    Y[c + 1] = X[c + 1].real
+    return np.fft.irfft(Y, n=N)
+
+
+@pytest.mark.parametrize("N,c", [(360, 4), (180, 3), (720, 8), (96, 1)])
+def test_filter_matches_fftpack_packing(N, c):
+    M = 31
+    o = OracleModel(N, M, 100.0, cutoff=[c])
+    rng = np.random.default_rng(N + c)
+    x = np.zeros(N + 4)
+    x[2:-2] = rng.standard_normal(N)
+    y = o.filter_row(0, 2, x)  # full row Fortran 2 is flagged by cutoff entry 1
+    ref = fftpack_projection(x[2:-2], c)
+    assert np.max(np.abs(y[2:-2] - ref)) < 1e-13 * np.max(np.abs(x))
+    # halos untouched
+    assert np.all(y[:2] == 0) and np.all(y[-2:] == 0)
+
+
+def test_filter_kept_modes():
+    N, c = 360, 4
+    o = OracleModel(N, 31, 100.0, cutoff=[c])
+    lam = 2 * np.pi * np.arange(N) / N
+    def run(f):
+        x = np.zeros(N + 4)
+        x[2:-2] = f
+        return o.filter_row(0, 2, x)[2:-2]
+    for k in range(0, c + 1):
+        assert np.allclose(run(np.cos(k * lam)), np.cos(k * lam), atol=1e-13)
+        assert np.allclose(run(np.sin(k * lam)), np.sin(k * lam), atol=1e-13)
+    # the cosine of wavenumber c+1 passes, its sine does not (quirk of the
+    # factor indices 1..2(c+1), src/filter_mod.F90:79-84)
+    assert np.allclose(run(np.cos((c + 1) * lam)), np.cos((c + 1) * lam), atol=1e-13)
+    assert np.allclose(run(np.sin((c + 1) * lam)), 0, atol=1e-13)
+    for k in (c + 2, c + 7, N // 2 - 1):
+        assert np.allclose(run(np.cos(k * lam)), 0, atol=1e-13)
+        assert np.allclose(run(np.sin(k * lam)), 0, atol=1e-13)
+
+
+def test_filter_row_sets():
+    """South filters half rows 1..n, north only n-1 half rows (the flag
+    index of src/filter_mod.F90:56 is one past the factor index of :95)."""
+    N, M, n = 360, 181, 5
+    o = OracleModel(N, M, 240.0, cutoff=[4] * n)
+    ff, fh, cf, ch = o.filter_flags()
+    assert [j for j in range(M) if ff[j]] == list(range(1, n + 1)) + list(range(M - 1 - n, M - 1))
+    assert [j for j in range(M - 1) if fh[j]] == list(range(0, n)) + list(range(M - n, M - 1))
+    assert all(cf[j] == 4 for j in range(M) if ff[j])
+    assert all(ch[j] == 4 for j in range(M - 1) if fh[j])
+    # a half row whose factor row is unset keeps nothing
+    o2 = OracleModel(N, M, 240.0, cutoff=[4, 0, 3])
+    ff, fh, cf, ch = o2.filter_flags()
+    assert fh[M - 3] == 1 and ch[M - 3] == -1  # flagged by entry 3, factors of entry 2 (zero)
+
+
+def _seeded(N, M, seed=0):
+    import gdc
+    return gdc.ic_seeded(N, M, seed=seed)
+
+
+@pytest.mark.parametrize("split", [0, 2, 3])
+def test_mass_conserved_without_filter(split):
+    """With the filter and diffusion off the flux-form mass divergence and
+    its pole caps telescope: total mass is conserved to round-off."""
+    N, M = 72, 37
+    u, v, gd, ghs = _seeded(N, M, seed=3)
+    o = OracleModel(N, M, 600.0, subcycles=4, split_scheme=split, use_zonal_tend_filter=0, cutoff=[])
+    o.set_state(u, v, gd, ghs)
+    m0, _, _ = o.diag()
+    assert o.step(12) == 0
+    m1, _, _ = o.diag()
+    assert abs(m1 - m0) / m0 < 1e-13
+
+
+def test_antisymmetry_identities():
+    """check_antisymmetry's four sums vanish to round-off relative to the
+    magnitudes of the terms they combine (filter off)."""
+    N, M = 72, 37
+    u, v, gd, ghs = _seeded(N, M, seed=5)
+    o = OracleModel(N, M, 600.0, use_zonal_tend_filter=0, cutoff=[])
+    o.set_state(u, v, gd, ghs)
+    du, dv, dgd = o.tendency(0)
+    s = o.antisymmetry()
+    scale = np.sqrt(np.sum(interior(du) ** 2) + np.sum(interior(dv) ** 2)) * 1e4 * N * M
+    assert np.all(np.abs(s) < 1e-10 * scale), s
+
+
+def test_energy_conserving_without_filter():
+    """The quadratic-conservation beta keeps total energy nearly constant
+    (the design goal of the IAP scheme); with qcon off it drifts more."""
+    N, M = 72, 37
+    u, v, gd, ghs = _seeded(N, M, seed=7)
+    def drift(qcon):
+        o = OracleModel(N, M, 300.0, subcycles=4, split_scheme=0, qcon_modified=qcon, use_zonal_tend_filter=0,
+                        cutoff=[])
+        o.set_state(u, v, gd, ghs)
+        _, e0, _ = o.diag()
+        o.step(20)
+        _, e1, b = o.diag()
+        return abs(e1 - e0) / e0, b
+    d_on, b_on = drift(1)
+    d_off, b_off = drift(0)
+    assert d_on < 1e-10
+    assert b_off == 1.0 and b_on != 1.0
+
+
+def test_steady_geostrophic_stays_steady():
+    import gdc
+    N, M = 72, 37
+    u, v, gd, ghs = gdc.ic_steady_geostrophic(N, M)
+    o = OracleModel(N, M, 600.0, subcycles=4, split_scheme=2, cutoff=[3, 3])
+    o.set_state(u, v, gd, ghs)
+    o.step(24)
+    s = o.get_state()
+    err = np.sqrt(np.mean((interior(s["gd"]) - interior(gd)) ** 2)) / np.mean(interior(gd))
+    assert err < 1e-3, err  # truncation error of a 5-degree grid after 4 hours
