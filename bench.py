@@ -259,7 +259,7 @@ def cpu_baseline_sample(seconds_target=12.0):
     from oracle.oracle import OracleModel
     N, M, dt, _, cut = GRIDS[360]
     ic = gdc.ic_seeded(N, M, seed=0)
-    o = OracleModel(N, M, dt, subcycles=6, split_scheme=2, qcon_modified=1, cutoff=cut)
+    o = OracleModel(N, M, dt, subcycles=6, split_scheme=2, qcon_modified=1, cutoff=cut, fast=True)
     o.set_state(*ic)
     t0 = time.perf_counter()
     o.step(2)
@@ -269,7 +269,8 @@ def cpu_baseline_sample(seconds_target=12.0):
     o.step(n)
     t = time.perf_counter() - t0
     return {"value": N * M * n / t, "unit": "grid-pt-steps/s", "cores": 1, "kind": "port",
-            "sample": f"oracle (C restatement of the reference, FP64, 1 thread): one 360x181 member, {n} csp2 steps"}
+            "sample": f"oracle port of the reference (FP64, plain sums, -Ofast as the reference's build, "
+                      f"1 thread): one 360x181 member, {n} csp2 steps"}
 
 
 def run_ours(args, rank, world, dist):
@@ -366,7 +367,7 @@ def _ref_member(task):
     N, M, dt, nst, cut, seed = task["N"], task["M"], task["dt"], task["nsteps"], task["cutoff"], task["seed"]
     u, v, gd, ghs = gdc.ic_seeded(N, M, seed=0)
     gd = gdc.ic_add_noise(gd.copy(), N, M, seed=seed, sigma=1.0 * G)
-    o = OracleModel(N, M, dt, subcycles=6, split_scheme=2, qcon_modified=1, cutoff=cut)
+    o = OracleModel(N, M, dt, subcycles=6, split_scheme=2, qcon_modified=1, cutoff=cut, fast=True)
     o.set_state(u, v, gd, ghs)
     o.step(nst)
     return N * M * nst
@@ -402,7 +403,7 @@ def run_reference(args, rank, world, dist):
             done += sum(pool.map(_ref_member, tasks))
         t = time.perf_counter() - t0
     value = done / t
-    sample = (f"oracle port (FP64 C restatement of the reference), {cores} processes over the 64-member ensemble, "
+    sample = (f"oracle port of the reference (FP64, plain sums, -Ofast), {cores} processes over the 64-member ensemble, "
               f"{rounds} round(s) of 8/4/2 steps per 180x91/360x181/720x361 member")
     print(json.dumps({
         "impl": "reference",

@@ -67,13 +67,16 @@ def build(force: bool = False, verbose: bool = False) -> Path:
             objs.append(obj)
             # The FP64 unit keeps the reference's rounding: no FMA contraction.
             fmad = ["--fmad=false"] if src.stem.endswith("_f64") else []
-            cmds.append([nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", *fmad, "-Xcompiler", "-fPIC",
-                         f"-I{INCLUDE}", "-c", str(src), "-o", str(obj)])
+            cmds.append([nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", *fmad, "-Xcompiler",
+                         "-fPIC,-ffp-contract=off", f"-I{INCLUDE}", "-c", str(src), "-o", str(obj)])
         for src in cpp:
             obj = OUT / (src.stem + ".o")
             objs.append(obj)
-            cmds.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", f"-I{cuda / 'include'}",
-                         f"-I{INCLUDE}", "-c", str(src), "-o", str(obj)])
+            # No FMA contraction in host code: the mesh and coefficient tables
+            # round exactly as the reference's (and the same on x86 and Arm,
+            # where g++ contracts by default).
+            cmds.append(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-Wall",
+                         f"-I{cuda / 'include'}", f"-I{INCLUDE}", "-c", str(src), "-o", str(obj)])
         if verbose:
             for c in cmds:
                 print(" ".join(c))
@@ -83,7 +86,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     drv_src = CSRC / "dycore_test.cpp"
     drv = OUT / "dycore_test"
     if drv_src.exists() and (force or _stale(drv, [drv_src, lib])):
-        _run_all([["g++", "-O2", "-std=c++17", "-Wall", f"-I{INCLUDE}", str(drv_src), "-o", str(drv),
+        _run_all([["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-Wall", f"-I{INCLUDE}", str(drv_src), "-o", str(drv),
                    f"-L{OUT}", "-lgdc", f"-Wl,-rpath,{OUT}"]])
     return lib
 

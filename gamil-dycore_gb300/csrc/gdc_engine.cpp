@@ -16,6 +16,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "gdc_internal.h"
@@ -33,7 +34,7 @@ bool uses_isp(const gdc_params& p) { return p.split_scheme == GDC_SPLIT_ISP; }
 
 // Byte layout of one member's device allocation.
 struct Layout {
-  size_t st[SL_N][3], lo[SL_N][3], td[TS_N][3], ghs, coef, twid, rowinfo, dcoef, total;
+  size_t st[SL_N][3], lo[SL_N][3], td[TS_N][3], ghs, coef, twid, rowinfo, dcoef, given_u, given_v, total;
 };
 
 template <typename T>
@@ -63,6 +64,8 @@ Layout make_layout(const gdc_params& p, int N, int M) {
   L.twid = take(2 * (size_t)N * sizeof(T));
   L.rowinfo = take((size_t)M * sizeof(int));
   L.dcoef = take((size_t)(3 * M) * sizeof(double));
+  L.given_u = take(full * sizeof(T));
+  L.given_v = take(half * sizeof(T));
   L.total = off;
   return L;
 }
@@ -126,12 +129,13 @@ class Batch final : public BatchIface {
     if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("cudaStreamCreate", e));
     stream = own_stream;
     if (int rc = dalloc((void**)&d_mem, sizeof(MemberDev<T>) * kSlots)) return rc;
-    if (int rc = dalloc((void**)&d_counters, sizeof(unsigned) * kSlots)) return rc;
+    if (int rc = dalloc((void**)&d_active, sizeof(int) * kSlots)) return rc;
+    if (int rc = dalloc((void**)&d_uvslot, sizeof(int) * kSlots)) return rc;
+    cudaMemset(d_uvslot, 0xff, sizeof(int) * kSlots);  // -1: no given u, v
     if (int rc = dalloc((void**)&d_beta, sizeof(double) * kSlots)) return rc;
     if (int rc = dalloc((void**)&d_diag, sizeof(double) * 3 * kSlots)) return rc;
     if (int rc = dalloc((void**)&d_steps, sizeof(long long) * kSlots)) return rc;
     if (int rc = dalloc((void**)&d_nan, sizeof(long long) * kSlots)) return rc;
-    cudaMemset(d_counters, 0, sizeof(unsigned) * kSlots);
     cudaMemset(d_beta, 0, sizeof(double) * kSlots);
     cudaMemset(d_diag, 0, sizeof(double) * 3 * kSlots);
     cudaMemset(d_steps, 0, sizeof(long long) * kSlots);
@@ -140,7 +144,7 @@ class Batch final : public BatchIface {
     hdesc.resize(kSlots);
     std::memset(hdesc.data(), 0, sizeof(MemberDev<T>) * kSlots);
     tile_r = 8;
-    tile_c = 32;
+    tile_c = default_cols();
     e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("init", e));
     return GDC_OK;
@@ -285,6 +289,8 @@ class Batch final : public BatchIface {
     d.twid = (const T*)(base + L.twid);
     d.rowinfo = (const int*)(base + L.rowinfo);
     d.dcoef = (const double*)(base + L.dcoef);
+    d.given_u = (T*)(base + L.given_u);
+    d.given_v = (T*)(base + L.given_v);
     // Upload (synchronously: admission is a step-boundary operation).
     sync_stream();
     e = cudaMemset(r.dmem, 0, L.total);
@@ -297,6 +303,18 @@ class Batch final : public BatchIface {
     if (e == cudaSuccess) e = upload_field(d.st[lvl][F_GD], d.lo[lvl][F_GD], hg);
     if (e == cudaSuccess) e = upload_field(d.st[lvl][F_IU], d.lo[lvl][F_IU], hu);
     if (e == cudaSuccess) e = upload_field(d.st[lvl][F_IV], d.lo[lvl][F_IV], hv);
+    {
+      // The initial condition's own u, v: the first stage reads them as
+      // given (state(1)%u, %v in the reference), not re-derived.
+      std::vector<double> gu(full), gv(half);
+      for (int j = 0; j < M; ++j)
+        for (int i = 0; i < N; ++i) gu[(size_t)j * N + i] = at(u, i, j);
+      for (int j = 0; j < Mh; ++j)
+        for (int i = 0; i < N; ++i) gv[(size_t)j * N + i] = at(v, i, j);
+      if (e == cudaSuccess) e = upload_field(d.given_u, nullptr, gu);
+      if (e == cudaSuccess) e = upload_field(d.given_v, nullptr, gv);
+      if (e == cudaSuccess) e = cudaMemcpy(d_uvslot + slot, &lvl, sizeof(int), cudaMemcpyHostToDevice);
+    }
     if (e == cudaSuccess) e = cudaMemcpy(d_mem + slot, &d, sizeof(d), cudaMemcpyHostToDevice);
     const long long minus1 = -1, zero = 0;
     if (e == cudaSuccess) e = cudaMemcpy(d_nan + slot, &minus1, sizeof(minus1), cudaMemcpyHostToDevice);
@@ -443,7 +461,9 @@ class Batch final : public BatchIface {
     put(iu, M, [&](int i, int j) { return hu[(size_t)j * N + i]; });
     put(iv, Mh, [&](int i, int j) { return hv[(size_t)j * N + i]; });
     put(ig, M, [&](int i, int j) { return sg[(size_t)j * N + i]; });
-    if (r.steps_done == 0) {
+    int uvs = -1;
+    cudaMemcpy(&uvs, d_uvslot + id, sizeof(int), cudaMemcpyDeviceToHost);
+    if (r.steps_done == 0 && std::is_same<T, double>::value) {
       // state(old) still holds the initial condition's own u and v.
       auto copy_ic = [&](double* f, const std::vector<double>& src, int rows) {
         if (!f) return;
@@ -452,6 +472,14 @@ class Batch final : public BatchIface {
       };
       copy_ic(u, r.ic_u, M);
       copy_ic(v, r.ic_v, Mh);
+    } else if (uvs == lvl && (u || v)) {
+      // u, v held as given with this level (after diffusion).
+      std::vector<double> gu, gv;
+      e = download_field(d.given_u, nullptr, (size_t)M * N, gu);
+      if (e == cudaSuccess) e = download_field(d.given_v, nullptr, (size_t)Mh * N, gv);
+      if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("get_state: u, v", e));
+      put(u, M, [&](int i, int j) { return gu[(size_t)j * N + i]; });
+      put(v, Mh, [&](int i, int j) { return gv[(size_t)j * N + i]; });
     } else {
       // update_state's recovery of u and v (src/dycore_mod.F90:636-645).
       put(u, M, [&](int i, int j) {
@@ -481,10 +509,10 @@ class Batch final : public BatchIface {
   int set_tile(int r, int c) override {
     if (r == 0 && c == 0) {
       r = 8;
-      c = 32;
+      c = default_cols();
     }
-    if (r < 1 || r > 32 || c < 8 || c > 256 || r * c > 4096)
-      return fail(GDC_E_CONFIG, "set_tile: rows in 1..32, cols in 8..256, rows*cols <= 4096");
+    if (r < 1 || r > 32 || c < 8 || c > 256 || r * c > 512)
+      return fail(GDC_E_CONFIG, "set_tile: rows in 1..32, cols in 8..256, rows*cols <= 512");
     tile_r = r;
     tile_c = c;
     dirty = true;
@@ -501,7 +529,7 @@ class Batch final : public BatchIface {
   // Times each candidate tile shape on the current members (graph replay,
   // CUDA events) and keeps the fastest.  Advances the members.
   int autotune(int* rr, int* cc, double* best_ms) override {
-    static const int cand[][2] = {{4, 32}, {8, 32}, {16, 32}, {4, 64}, {8, 64}, {2, 128}, {4, 128}, {16, 16}};
+    static const int cand[][2] = {{4, 32}, {8, 32}, {16, 32}, {4, 64}, {8, 64}, {2, 128}, {4, 128}, {16, 16}, {2, 256}};
     double best = 1e30;
     int br = tile_r, bc = tile_c;
     for (auto& c : cand) {
@@ -623,7 +651,8 @@ class Batch final : public BatchIface {
   gdc_params P;
   cudaStream_t own_stream = nullptr, stream = nullptr;
   MemberDev<T>* d_mem = nullptr;
-  unsigned* d_counters = nullptr;
+  int* d_active = nullptr;  // slots of the active members (beta / diag blocks)
+  int* d_uvslot = nullptr;  // per member: level whose u, v are held as given (-1 none)
   double* d_beta = nullptr;
   double* d_diag = nullptr;
   long long* d_steps = nullptr;
@@ -643,6 +672,10 @@ class Batch final : public BatchIface {
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
   std::vector<Prof> prof;
   std::vector<void*> allocs;
+
+  // FP32 is bandwidth-bound: larger tiles amortise the halo; FP64 is
+  // arithmetic-bound: smaller tiles spread the rows over more SMs.
+  static int default_cols() { return sizeof(T) == 4 ? 64 : 32; }
 
   int fail(int code, const std::string& m) {
     err = m;
@@ -766,11 +799,13 @@ class Batch final : public BatchIface {
       if (d_partials) cudaFree(d_partials);
       d_partials = nullptr;
       part_cap = std::max<size_t>(pc, 2 * part_cap);
-      cudaError_t e = cudaMalloc(&d_partials, part_cap * 2 * sizeof(double));
+      cudaError_t e = cudaMalloc(&d_partials, part_cap * 4 * sizeof(double));
       if (e != cudaSuccess) return fail(GDC_E_OOM, cuda_msg("rebuild: partials", e));
     }
     cudaError_t e = cudaSuccess;
     if (nwork) e = cudaMemcpy(d_wl, hwl.data(), nwork * sizeof(WorkItem), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !active_slots.empty())
+      e = cudaMemcpy(d_active, active_slots.data(), active_slots.size() * sizeof(int), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(d_mem, hdesc.data(), sizeof(MemberDev<T>) * kSlots, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("rebuild: upload", e));
     dirty = false;
@@ -788,12 +823,12 @@ class Batch final : public BatchIface {
     a.h_scale = 0.5;
     a.ip_slot = -1;
     a.partials = d_partials;
-    a.counters = d_counters;
     a.beta = d_beta;
     a.qcon = P.qcon_modified;
     a.ub_lon = P.uv_adv_upwind_lon_beta;
     a.ub_lat = P.uv_adv_upwind_lat_beta;
     a.rescale_rtol = P.filter_rescale_rtol;
+    a.uvslot = d_uvslot;
     return a;
   }
 
@@ -811,6 +846,21 @@ class Batch final : public BatchIface {
       pr->push_back(Prof{0, e0, e1});
     }
     return rc ? fail(rc, "stage launch failed") : GDC_OK;
+  }
+  int run_beta(int beta_mode, std::vector<Prof>* pr) {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (pr) {
+      cudaEventCreate(&e0);
+      cudaEventCreate(&e1);
+      cudaEventRecord(e0, stream);
+    }
+    int rc = launch_beta<T>(d_mem, d_active, (int)active_slots.size(), d_partials, d_beta, P.qcon_modified,
+                            beta_mode, stream);
+    if (pr) {
+      cudaEventRecord(e1, stream);
+      pr->push_back(Prof{1, e0, e1});
+    }
+    return rc ? fail(rc, "beta launch failed") : GDC_OK;
   }
   int run_final(const FinalArgs& a, std::vector<Prof>* pr) {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -845,7 +895,8 @@ class Batch final : public BatchIface {
     a.tout = TS_NEW;
     a.tprev = TS_OLD;
     a.do_ip = 1;
-    if (int rc = run_stage(a, pr)) return rc;  // correct + beta
+    if (int rc = run_stage(a, pr)) return rc;  // correct
+    if (int rc = run_beta(0, pr)) return rc;   // beta
     FinalArgs f;
     f.base_slot = o;
     f.out_slot = n;
@@ -854,6 +905,7 @@ class Batch final : public BatchIface {
     f.use_lo = sizeof(T) == 4 ? 1 : 0;
     f.h_scale = 1.0;
     f.beta = d_beta;
+    f.uvslot = d_uvslot;
     return run_final(f, pr);
   }
 
@@ -906,6 +958,7 @@ class Batch final : public BatchIface {
     a.beta_mode = 1;
     a.ip_slot = SL_SAVED;
     if (int rc = run_stage(a, pr)) return rc;
+    if (int rc = run_beta(1, pr)) return rc;
     FinalArgs f;
     f.base_slot = SL_SAVED;
     f.out_slot = new_;
@@ -914,6 +967,7 @@ class Batch final : public BatchIface {
     f.use_lo = sizeof(T) == 4 ? 1 : 0;
     f.h_scale = 0.5;
     f.beta = d_beta;
+    f.uvslot = d_uvslot;
     return run_final(f, pr);
   }
 
@@ -943,7 +997,7 @@ class Batch final : public BatchIface {
         cudaEventCreate(&e1);
         cudaEventRecord(e0, stream);
       }
-      rc = launch_diffusion<T>(d_mem, d_wl, nwork, tile_r, tile_c, max_n, new_, c, stream);
+      rc = launch_diffusion<T>(d_mem, d_wl, nwork, tile_r, tile_c, max_n, new_, c, d_uvslot, stream);
       if (pr) {
         cudaEventRecord(e1, stream);
         pr->push_back(Prof{3, e0, e1});
@@ -953,8 +1007,8 @@ class Batch final : public BatchIface {
     // diag_run(state(old)) after time_advance (src/dycore_mod.F90:135).
     DiagArgs d;
     d.slot = new_;
+    d.count_step = 1;
     d.partials = d_partials;
-    d.counters = d_counters;
     d.diag = d_diag;
     d.beta = d_beta;
     d.steps = d_steps;
@@ -965,7 +1019,7 @@ class Batch final : public BatchIface {
       cudaEventCreate(&e1);
       cudaEventRecord(e0, stream);
     }
-    rc = launch_diag<T>(d_mem, d_wl, nwork, d, stream);
+    rc = launch_diag<T>(d_mem, d_wl, nwork, d_active, (int)active_slots.size(), d, stream);
     if (pr) {
       cudaEventRecord(e1, stream);
       pr->push_back(Prof{2, e0, e1});
@@ -981,29 +1035,31 @@ class Batch final : public BatchIface {
     append_items(slot, wl, pc);
     WorkItem* dwl = nullptr;
     double* dpart = nullptr;
+    int* dslot = nullptr;
     if (cudaMalloc(&dwl, sizeof(WorkItem) * wl.size()) != cudaSuccess ||
-        cudaMalloc(&dpart, sizeof(double) * 2 * wl.size()) != cudaSuccess) {
+        cudaMalloc(&dpart, sizeof(double) * 4 * wl.size()) != cudaSuccess ||
+        cudaMalloc(&dslot, sizeof(int)) != cudaSuccess) {
       cudaGetLastError();
       if (dwl) cudaFree(dwl);
+      if (dpart) cudaFree(dpart);
       return fail(GDC_E_OOM, "initial diag: cudaMalloc");
     }
     cudaMemcpy(dwl, wl.data(), sizeof(WorkItem) * wl.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(dslot, &slot, sizeof(int), cudaMemcpyHostToDevice);
     cudaMemcpy(d_mem + slot, &hdesc[slot], sizeof(MemberDev<T>), cudaMemcpyHostToDevice);
     DiagArgs d;
     d.slot = old_;
+    d.count_step = 0;  // the initial diag is not a step
     d.partials = dpart;
-    d.counters = d_counters;
     d.diag = d_diag;
     d.beta = nullptr;
     d.steps = d_steps;
     d.nan_step = d_nan;
-    int rc = launch_diag<T>(d_mem, dwl, (int)wl.size(), d, stream);
+    int rc = launch_diag<T>(d_mem, dwl, (int)wl.size(), dslot, 1, d, stream);
     cudaError_t e = cudaStreamSynchronize(stream);
-    // The initial diag is not a step: reset the step counter.
-    const long long zero = 0;
-    cudaMemcpy(d_steps + slot, &zero, sizeof(zero), cudaMemcpyHostToDevice);
     cudaFree(dwl);
     cudaFree(dpart);
+    cudaFree(dslot);
     hdesc[slot].pbase = saved.pbase;
     hdesc[slot].pcount = saved.pcount;
     if (rc || e != cudaSuccess) return fail(GDC_E_CUDA, "initial diag failed");

@@ -104,6 +104,8 @@ struct MemberDev {
   const T* twid;          // cos(2 pi m/N), m<N, then sin(2 pi m/N)
   const int* rowinfo;
   const double* dcoef;    // FP64 diag weights: mass weight [M], full cos [M], half cos [Mh]
+  T* given_u;             // u and v supplied with the state of level uvslot[member]
+  T* given_v;             // (initial condition, diffusion) rather than derived
 };
 
 enum Field { F_GD = 0, F_IU = 1, F_IV = 2 };
@@ -137,12 +139,12 @@ struct StageArgs {
   int do_ip;                         // form partials and beta
   int beta_mode;                     // 0 predict_correct, 1 isp
   int ip_slot;                       // state slot for beta_mode 1
-  double* partials;                  // 2 doubles per partial slot
-  unsigned* counters;                // per member, last-block detection
+  double* partials;                  // 4 doubles per partial slot
   double* beta;                      // per member
   int qcon;
   double ub_lon, ub_lat;             // uv_adv_upwind_{lon,lat}_beta
   double rescale_rtol;               // gdc_params::filter_rescale_rtol
+  int* uvslot;                       // per member: slot whose u, v are given (-1 none)
 };
 
 struct FinalArgs {
@@ -151,12 +153,13 @@ struct FinalArgs {
   int use_lo;          // write compensated result (time level)
   double h_scale;      // step = pcdt[pass] * h_scale * beta (or * 1)
   const double* beta;  // per member or null
+  int* uvslot;         // per member; cleared when out_slot overwrites that level
 };
 
 struct DiagArgs {
   int slot;
-  double* partials;      // 2 doubles per partial slot
-  unsigned* counters;
+  int count_step;        // 1: this diag closes a model step
+  double* partials;      // 4 doubles per partial slot
   double* diag;          // per member: mass, energy, beta
   const double* beta;
   long long* steps;      // per member: steps completed (incremented here)
@@ -170,14 +173,20 @@ int launch_stage(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int adv
 template <typename T>
 int launch_final(const MemberDev<T>* mem, const WorkItem* wl, int nwork, const FinalArgs& a,
                  void* stream);
+// Per-item partial sums, then one block per member (`slots`) forms the totals.
 template <typename T>
-int launch_diag(const MemberDev<T>* mem, const WorkItem* wl, int nwork, const DiagArgs& a,
-                void* stream);
+int launch_diag(const MemberDev<T>* mem, const WorkItem* wl, int nwork, const int* slots,
+                int nmembers, const DiagArgs& a, void* stream);
+// beta of each member in `slots` from the stage kernel's partials.
+template <typename T>
+int launch_beta(const MemberDev<T>* mem, const int* slots, int nmembers, const double* partials,
+                double* beta, int qcon, int beta_mode, void* stream);
 // ordinary_diffusion (order 2): Laplacians of state `slot` into SA as
 // (gd', u', v'), then iap_transform of SA back into `slot`.
 template <typename T>
 int launch_diffusion(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int tile_rows,
-                     int tile_cols, int max_n, int slot, double sign_dt_coef, void* stream);
+                     int tile_cols, int max_n, int slot, double sign_dt_coef, int* uvslot,
+                     void* stream);
 template <typename T>
 int launch_copy_state(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int from_slot,
                       int to_slot, void* stream);

@@ -10,13 +10,21 @@
 // divergence is a zonal sum, and rows the zonal filter touches, whose
 // filter and s1/s2 rescale need the complete latitude circle).
 //
-// A work item stages gd, ghs, iap u, iap v of its rows +-1 (+2 for gd) and
-// columns +-1 (+2) in shared memory, derives iap gd = sqrt(gd),
+// A work item copies gd, ghs, iap u, iap v of its rows +-1 (+2 for gd) and
+// columns +-1 (+2) into shared memory with cp.async (every load of the
+// tile in flight at once; rows off the sphere are zero-filled, as the
+// reference's never-filled latitude halo), derives iap gd = sqrt(gd),
 // u = 2 iap_u / (iap_gd(i) + iap_gd(i+1)) and v = 2 iap_v / (iap_gd(j) +
 // iap_gd(j+1)) there (the update_state epilogue of the reference,
 // src/dycore_mod.F90:617-645, moved to the consumer so that only
 // {gd, iap u, iap v} live in HBM), then evaluates the operators point-wise
 // in the reference's order of operations.
+//
+// Sums: in FP64 every reduction the reference performs (filter s1/s2 and
+// projections, pole caps, beta's inner products, the diagnostics) is
+// accumulated in double-double and rounded once, i.e. it is the correctly
+// rounded sum of the reference's (rounded) terms, independent of the order
+// the GPU adds them in.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -31,34 +39,100 @@ namespace gdc {
 constexpr int kThreads = 256;
 constexpr int kRowChunk = 128;  // columns per chunk of a whole-row task
 constexpr int kMaxKeep = 128;   // packed FFT coefficients a filter row may keep
+constexpr int kPPT = 2;         // tile points per thread (tile <= 512 points)
 
 // ------------------------------------------------------------ helpers
 
+// Sum accumulator: double-double (Knuth TwoSum, exact without FMA) for
+// FP64, plain float for FP32.
+template <typename T>
+struct Acc;
+template <>
+struct Acc<double> {
+  double s = 0, c = 0;
+  __device__ void add(double x) {
+    const double t = s + x;
+    const double bp = t - s;
+    c += (s - (t - bp)) + (x - bp);
+    s = t;
+  }
+  __device__ void merge(double os, double oc) {
+    add(os);
+    c += oc;
+  }
+  __device__ double value() const { return s + c; }
+};
+template <>
+struct Acc<float> {
+  float s = 0, c = 0;
+  __device__ void add(float x) { s += x; }
+  __device__ void merge(float os, float oc) { s += os + oc; }
+  __device__ float value() const { return s + c; }
+};
+
 template <typename A>
-__device__ A warp_sum(A v) {
+__device__ inline A warp_sum(A v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
 
-// Deterministic block-wide sum (fixed shuffle tree + fixed warp order).
-template <typename A>
-__device__ A block_sum(A v, A* red) {
-  v = warp_sum(v);
+template <typename T>
+__device__ inline void warp_acc(Acc<T>& a) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const T os = __shfl_xor_sync(0xffffffffu, a.s, o);
+    const T oc = __shfl_xor_sync(0xffffffffu, a.c, o);
+    a.merge(os, oc);
+  }
+}
+
+// Block-wide accumulation; `red` holds 64 T.  Every thread gets the result.
+template <typename T>
+__device__ Acc<T> block_acc(Acc<T> a, T* red) {
+  warp_acc(a);
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
   __syncthreads();
-  if (l == 0) red[w] = v;
-  __syncthreads();
-  if (w == 0) {
-    A s = (l < nw) ? red[l] : A(0);
-    s = warp_sum(s);
-    if (l == 0) red[0] = s;
+  if (l == 0) {
+    red[2 * w] = a.s;
+    red[2 * w + 1] = a.c;
   }
   __syncthreads();
-  A r = red[0];
+  if (w == 0) {
+    Acc<T> b;
+    if (l < nw) {
+      b.s = red[2 * l];
+      b.c = red[2 * l + 1];
+    }
+    warp_acc(b);
+    if (l == 0) {
+      red[0] = b.s;
+      red[1] = b.c;
+    }
+  }
+  __syncthreads();
+  Acc<T> r;
+  r.s = red[0];
+  r.c = red[1];
   __syncthreads();
   return r;
 }
+
+template <typename T>
+__device__ inline T block_value(Acc<T> a, T* red) {
+  return block_acc(a, red).value();
+}
+
+// 4- or 8-byte asynchronous global->shared copy; src-size 0 zero-fills.
+template <typename T>
+__device__ __forceinline__ void cp_async(T* smem, const T* gmem, bool valid) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  const int n = valid ? (int)sizeof(T) : 0;
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(s), "l"(gmem), "n"(sizeof(T)),
+               "r"(n)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 template <typename T>
 struct TileSmem {
@@ -76,7 +150,7 @@ __device__ inline T ch(const MemberDev<T>& md, int k, int jh) {  // jh in -1..Mh
   return md.coef[ch_off(k, md.M) + jh + 1];
 }
 
-// Partition of a staging buffer of `words` T values into the seven arrays.
+// Partition of a staging buffer into the seven tile arrays.
 template <typename T>
 __device__ TileSmem<T> carve_tile(T* base, int R, int W, int j0, int i0) {
   TileSmem<T> t;
@@ -97,13 +171,13 @@ __device__ TileSmem<T> carve_tile(T* base, int R, int W, int j0, int i0) {
   return t;
 }
 
-// Load rows j0-1 .. j0+R+1 (full) and half rows j0-1 .. j0+R+1, columns
-// i0-1 .. i0+W+1 (periodic), then derive iap gd, u and v.  Rows outside
-// the sphere are the reference's never-filled latitude halo: 0.
+// Issue the copies of rows j0-1 .. j0+R+1 (full and half), columns
+// i0-1 .. i0+W+1 (periodic) into the tile; completes at cp_async_wait_all.
+// With `given`, u and v are copied too (the level's u, v were supplied
+// with its state instead of being derived from it).
 template <typename T>
-__device__ void stage_tile(const MemberDev<T>& md, const T* __restrict__ gd,
-                           const T* __restrict__ iu, const T* __restrict__ iv, TileSmem<T>& t,
-                           bool u_halo_row = false) {
+__device__ void tile_issue(const MemberDev<T>& md, const T* __restrict__ gd, const T* __restrict__ iu,
+                           const T* __restrict__ iv, TileSmem<T>& t, bool given = false) {
   const int N = md.N, M = md.M, Mh = md.Mh;
   const int SW = t.SW, n = t.rows * SW;
   for (int p = threadIdx.x; p < n; p += blockDim.x) {
@@ -111,24 +185,31 @@ __device__ void stage_tile(const MemberDev<T>& md, const T* __restrict__ gd,
     const int j = t.j0 - 1 + rr;
     int i = t.i0 - 1 + cc;
     i = i < 0 ? i + N : (i >= N ? i - N : i);
-    T g = 0, gh = 0, a = 0, b = 0;
-    if (j >= 0 && j < M) {
-      const size_t o = (size_t)j * N + i;
-      g = gd[o];
-      gh = md.ghs[o];
-      a = iu[o];
-      if (j < Mh) b = iv[o];
+    const bool vf = (j >= 0 && j < M), vh = (j >= 0 && j < Mh);
+    const size_t o = vf ? (size_t)j * N + i : 0;
+    cp_async(&t.gd[p], gd + o, vf);
+    cp_async(&t.ghs[p], md.ghs + o, vf);
+    cp_async(&t.iu[p], iu + o, vf);
+    cp_async(&t.iv[p], iv + (vh ? o : 0), vh);
+    if (given) {
+      cp_async(&t.u[p], md.given_u + o, vf);
+      cp_async(&t.v[p], md.given_v + (vh ? o : 0), vh);
     }
-    t.gd[p] = g;
-    t.ghs[p] = gh;
-    t.iu[p] = a;
-    t.iv[p] = b;
-    t.ig[p] = sqrt(g);
   }
+}
+
+// After the copies: iap gd everywhere, then u on full rows j0..j0+R (local
+// 1..R+1; from local 0 when the stencil also needs row j0-1), v on half
+// rows j0-1..j0+R (local 0..R+1), columns i0-1..i0+W (local 0..W+1).
+template <typename T>
+__device__ void tile_derive(const MemberDev<T>& md, TileSmem<T>& t, bool u_halo_row = false, bool given = false) {
+  const int M = md.M, Mh = md.Mh;
+  const int SW = t.SW, n = t.rows * SW;
+  cp_async_wait_all();
   __syncthreads();
-  // u on full rows j0..j0+R (local 1..R+1; from local 0 when the stencil
-  // also needs row j0-1), v on half rows j0-1..j0+R (local 0..R+1),
-  // columns i0-1..i0+W (local 0..W+1).
+  for (int p = threadIdx.x; p < n; p += blockDim.x) t.ig[p] = sqrt(t.gd[p]);
+  __syncthreads();
+  if (given) return;
   const int urow0 = u_halo_row ? 0 : 1;
   const int nd = (t.R + 2) * (t.W + 2);
   for (int q = threadIdx.x; q < nd; q += blockDim.x) {
@@ -144,12 +225,22 @@ __device__ void stage_tile(const MemberDev<T>& md, const T* __restrict__ gd,
   __syncthreads();
 }
 
+// Member descriptor copied to shared memory once per block.
+template <typename T>
+__device__ inline void load_member(const MemberDev<T>* __restrict__ mems, int member, MemberDev<T>* smd) {
+  const unsigned* src = reinterpret_cast<const unsigned*>(mems + member);
+  unsigned* dst = reinterpret_cast<unsigned*>(smd);
+  constexpr int nw = sizeof(MemberDev<T>) / 4;
+  for (int k = threadIdx.x; k < nw; k += blockDim.x) dst[k] = src[k];
+  __syncthreads();
+}
+
 // ----------------------------------------------------- point operators
-// (rr, cc) is the local position of full row j / half row j, column i.
+// p is the local position of full row j / half row j, column i.
 
 template <typename T, int PASS, int ADV>
-__device__ inline T point_du(const MemberDev<T>& md, const TileSmem<T>& t, int j, int p,
-                             T beta_lon, T beta_lat) {
+__device__ inline T point_du(const MemberDev<T>& md, const TileSmem<T>& t, int j, int p, T beta_lon,
+                             T beta_lat) {
   const int SW = t.SW;
   T r = 0;
   if (PASS != kFastPass) {
@@ -161,9 +252,8 @@ __device__ inline T point_du(const MemberDev<T>& md, const TileSmem<T>& t, int j
       adv_lon = cf(md, CF_RADVLON, j) * (u2 * t.iu[p + 1] - u1 * t.iu[p - 1]);
     } else {
       const T ic = t.iu[p], ip = t.iu[p + 1], im = t.iu[p - 1];
-      adv_lon = cf(md, CF_RADVLON, j) * (u2 * (ic + ip) - beta_lon * fabs(u2) * (ip - ic) -
-                                         u1 * (ic + im) + beta_lon * fabs(u1) * (ic - im) -
-                                         (u2 - u1) * ic);
+      adv_lon = cf(md, CF_RADVLON, j) * (u2 * (ic + ip) - beta_lon * fabs(u2) * (ip - ic) - u1 * (ic + im) +
+                                         beta_lon * fabs(u1) * (ic - im) - (u2 - u1) * ic);
     }
     // src/dycore_mod.F90:433-439 / :450-459
     const T v1 = (t.v[p - SW] + t.v[p - SW + 1]) * ch(md, CH_COS, j - 1);
@@ -173,17 +263,15 @@ __device__ inline T point_du(const MemberDev<T>& md, const TileSmem<T>& t, int j
       adv_lat = cf(md, CF_RADVLAT, j) * (v2 * t.iu[p + SW] - v1 * t.iu[p - SW]);
     } else {
       const T ic = t.iu[p], ip = t.iu[p + SW], im = t.iu[p - SW];
-      adv_lat = cf(md, CF_RADVLAT, j) * (v2 * (ic + ip) - beta_lat * fabs(v2) * (ip - ic) -
-                                         v1 * (ic + im) + beta_lat * fabs(v1) * (ic - im) -
-                                         (v2 - v1) * ic);
+      adv_lat = cf(md, CF_RADVLAT, j) * (v2 * (ic + ip) - beta_lat * fabs(v2) * (ip - ic) - v1 * (ic + im) +
+                                         beta_lat * fabs(v1) * (ic - im) - (v2 - v1) * ic);
     }
     r = -adv_lon - adv_lat;
   }
   if (PASS != kSlowPass) {
     // src/dycore_mod.F90:485-493
     const T fv = T(0.25) * (cf(md, CF_F, j) + cf(md, CF_C, j) * t.u[p]) *
-                 (cf(md, CF_C1, j) * (t.iv[p - SW] + t.iv[p - SW + 1]) +
-                  cf(md, CF_C2, j) * (t.iv[p] + t.iv[p + 1]));
+                 (cf(md, CF_C1, j) * (t.iv[p - SW] + t.iv[p - SW + 1]) + cf(md, CF_C2, j) * (t.iv[p] + t.iv[p + 1]));
     // src/dycore_mod.F90:514-519
     const T pgf = T(0.5) * (t.ig[p] + t.ig[p + 1]) / cf(md, CF_DLON, j) *
                   (t.gd[p + 1] + t.ghs[p + 1] - t.gd[p] - t.ghs[p]);
@@ -196,8 +284,8 @@ __device__ inline T point_du(const MemberDev<T>& md, const TileSmem<T>& t, int j
 }
 
 template <typename T, int PASS, int ADV>
-__device__ inline T point_dv(const MemberDev<T>& md, const TileSmem<T>& t, int jh, int p,
-                             T beta_lon, T beta_lat) {
+__device__ inline T point_dv(const MemberDev<T>& md, const TileSmem<T>& t, int jh, int p, T beta_lon,
+                             T beta_lat) {
   const int SW = t.SW;
   T r = 0;
   if (PASS != kFastPass) {
@@ -209,9 +297,8 @@ __device__ inline T point_dv(const MemberDev<T>& md, const TileSmem<T>& t, int j
       adv_lon = ch(md, CH_RADVLON, jh) * (u2 * t.iv[p + 1] - u1 * t.iv[p - 1]);
     } else {
       const T ic = t.iv[p], ip = t.iv[p + 1], im = t.iv[p - 1];
-      adv_lon = ch(md, CH_RADVLON, jh) * (u2 * (ic + ip) - beta_lon * fabs(u2) * (ip - ic) -
-                                          u1 * (ic + im) + beta_lon * fabs(u1) * (ic - im) -
-                                          (u2 - u1) * ic);
+      adv_lon = ch(md, CH_RADVLON, jh) * (u2 * (ic + ip) - beta_lon * fabs(u2) * (ip - ic) - u1 * (ic + im) +
+                                          beta_lon * fabs(u1) * (ic - im) - (u2 - u1) * ic);
     }
     // src/dycore_mod.F90:441-446 / :461-469
     const T vc = t.v[p] * ch(md, CH_COS, jh);
@@ -222,9 +309,8 @@ __device__ inline T point_dv(const MemberDev<T>& md, const TileSmem<T>& t, int j
       adv_lat = ch(md, CH_RADVLAT, jh) * (v2 * t.iv[p + SW] - v1 * t.iv[p - SW]);
     } else {
       const T ic = t.iv[p], ip = t.iv[p + SW], im = t.iv[p - SW];
-      adv_lat = ch(md, CH_RADVLAT, jh) * (v2 * (ic + ip) - beta_lat * fabs(v2) * (ip - ic) -
-                                          v1 * (ic + im) + beta_lat * fabs(v1) * (ic - im) -
-                                          (v2 - v1) * ic);
+      adv_lat = ch(md, CH_RADVLAT, jh) * (v2 * (ic + ip) - beta_lat * fabs(v2) * (ip - ic) - v1 * (ic + im) +
+                                          beta_lat * fabs(v1) * (ic - im) - (v2 - v1) * ic);
     }
     r = -adv_lon - adv_lat;
   }
@@ -233,8 +319,7 @@ __device__ inline T point_dv(const MemberDev<T>& md, const TileSmem<T>& t, int j
     const T f0 = cf(md, CF_F, jh), c0 = cf(md, CF_C, jh);
     const T f1 = cf(md, CF_F, jh + 1), c1 = cf(md, CF_C, jh + 1);
     const T fu = T(0.25) * ((f0 + c0 * t.u[p]) * t.iu[p] + (f0 + c0 * t.u[p - 1]) * t.iu[p - 1] +
-                            (f1 + c1 * t.u[p + SW]) * t.iu[p + SW] +
-                            (f1 + c1 * t.u[p + SW - 1]) * t.iu[p + SW - 1]);
+                            (f1 + c1 * t.u[p + SW]) * t.iu[p + SW] + (f1 + c1 * t.u[p + SW - 1]) * t.iu[p + SW - 1]);
     // src/dycore_mod.F90:530-535
     const T pgf = T(0.5) * (t.ig[p] + t.ig[p + SW]) / ch(md, CH_DLAT, jh) * ch(md, CH_COS, jh) *
                   (t.gd[p + SW] + t.ghs[p + SW] - t.gd[p] - t.ghs[p]);
@@ -252,8 +337,8 @@ __device__ inline T point_dgd(const MemberDev<T>& md, const TileSmem<T>& t, int 
   if (PASS == kSlowPass) return T(0);  // src/dycore_mod.F90:297
   const int SW = t.SW;
   // src/dycore_mod.F90:546-552
-  const T mdlon = ((t.ig[p] + t.ig[p + 1]) * t.iu[p] - (t.ig[p] + t.ig[p - 1]) * t.iu[p - 1]) *
-                  T(0.5) / cf(md, CF_DLON, j);
+  const T mdlon = ((t.ig[p] + t.ig[p + 1]) * t.iu[p] - (t.ig[p] + t.ig[p - 1]) * t.iu[p - 1]) * T(0.5) /
+                  cf(md, CF_DLON, j);
   // src/dycore_mod.F90:564-570
   const T mdlat = ((t.ig[p] + t.ig[p + SW]) * t.iv[p] * ch(md, CH_COS, j) -
                    (t.ig[p] + t.ig[p - SW]) * t.iv[p - SW] * ch(md, CH_COS, j - 1)) *
@@ -263,17 +348,18 @@ __device__ inline T point_dgd(const MemberDev<T>& md, const TileSmem<T>& t, int 
 
 // ------------------------------------------------------- consumers
 
-// Per-point consumer of one tendency value of field f at (row j, column i).
+// Consumer of one tendency value of field f at offset o.  `base` and
+// `prev` are the update operand and the previous tendency, supplied by the
+// caller (prefetched for bulk tiles).
 template <typename T>
 struct Emit {
   const MemberDev<T>& md;
   const StageArgs& a;
   T h, s2;
-  T ip1 = 0, ip2 = 0;
+  Acc<T> ip1, ip2;
   __device__ Emit(const MemberDev<T>& m, const StageArgs& s, T h_) : md(m), a(s), h(h_), s2(T(s.scale2)) {}
 
-  __device__ void put(int f, int j, int i, T val, T wcos) {
-    const size_t o = (size_t)j * md.N + i;
+  __device__ void put(int f, size_t o, T val, T wcos, T base, T prev) {
     if (a.taccum >= 0) {
       // add_data(tend, accum_fast_tend), src/dycore_mod.F90:721
       T* acc = md.td[a.taccum][f];
@@ -286,16 +372,19 @@ struct Emit {
     }
     if (a.tadd2 >= 0) val = val + md.td[a.tadd2][f][o] * s2;  // scale_data then add_data
     if (a.tout >= 0) md.td[a.tout][f][o] = val;
-    if (a.out_slot >= 0) {
-      // update_state, src/dycore_mod.F90:609-633 (new = old + dt * tend)
-      md.st[a.out_slot][f][o] = md.st[a.base_slot][f][o] + h * val;
-    }
+    // update_state, src/dycore_mod.F90:609-633 (new = old + dt * tend)
+    if (a.out_slot >= 0) md.st[a.out_slot][f][o] = base + h * val;
     if (a.do_ip) {
       // inner_product_tend_tend / _tend_state, src/types_mod.F90:347-397
-      const T pv = a.beta_mode == 0 ? md.td[a.tprev][f][o] : md.st[a.ip_slot][f][o];
-      ip1 += pv * val * wcos;
-      ip2 += val * val * wcos;
+      ip1.add(prev * val * wcos);
+      ip2.add(val * val * wcos);
     }
+  }
+  // Operands read straight from global memory (row tasks, isp modes).
+  __device__ T base_of(int f, size_t o) const { return a.out_slot >= 0 ? md.st[a.base_slot][f][o] : T(0); }
+  __device__ T prev_of(int f, size_t o) const {
+    if (!a.do_ip) return T(0);
+    return a.beta_mode == 0 ? md.td[a.tprev][f][o] : md.st[a.ip_slot][f][o];
   }
 };
 
@@ -313,16 +402,16 @@ __device__ void filter_project(const MemberDev<T>& md, T* x, int keep, T* coefs)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   __syncthreads();
   for (int p = warp; p < keep; p += nw) {
-    T acc = 0;
+    Acc<T> acc;
     if (p == 0) {
-      for (int n = lane; n < N; n += 32) acc += x[n];
+      for (int n = lane; n < N; n += 32) acc.add(x[n]);
     } else {
       const int k = (p + 1) >> 1;
       const T* tab = (p & 1) ? ctab : stab;
-      for (int n = lane; n < N; n += 32) acc += x[n] * tab[(k * n) % N];
+      for (int n = lane; n < N; n += 32) acc.add(x[n] * tab[(k * n) % N]);
     }
-    acc = warp_sum(acc);
-    if (lane == 0) coefs[p] = acc * (p == 0 ? T(1.0) / T(N) : T(2.0) / T(N));
+    warp_acc(acc);
+    if (lane == 0) coefs[p] = acc.value() * (p == 0 ? T(1.0) / T(N) : T(2.0) / T(N));
   }
   __syncthreads();
   for (int n = threadIdx.x; n < N; n += blockDim.x) {
@@ -344,73 +433,53 @@ __device__ void filter_project(const MemberDev<T>& md, T* x, int keep, T* coefs)
 // rtol > 0 (an extension; 0 is the reference) the rescale is skipped when
 // s1 or s2 is zero to within rtol of the sum of the magnitudes of its terms.
 template <typename T>
-__device__ void filter_rescale(const MemberDev<T>& md, T* x, const T* __restrict__ w1,
-                               const T* __restrict__ w2, int keep, T* coefs, T* red, double rtol) {
+__device__ void filter_rescale(const MemberDev<T>& md, T* x, const T* __restrict__ w1, const T* __restrict__ w2,
+                               int keep, T* coefs, T* red, double rtol) {
   const int N = md.N;
-  T s = 0, sa = 0;
+  Acc<T> s, sa;
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     const T t = x[i] * (w2 ? (w1[i] + w2[i]) : w1[i]);
-    s += t;
-    sa += fabs(t);
+    s.add(t);
+    sa.add(fabs(t));
   }
-  const T s1 = block_sum(s, red);
-  const T a1 = rtol > 0 ? block_sum(sa, red) : T(0);
+  const T s1 = block_value(s, red);
+  const T a1 = rtol > 0 ? block_value(sa, red) : T(0);
   if (!(fabs(s1) > T(1.0e-16))) return;  // src/filter_mod.F90:31
   filter_project(md, x, keep, coefs);
-  s = 0;
-  sa = 0;
+  Acc<T> q, qa;
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     const T t = x[i] * (w2 ? (w1[i] + w2[i]) : w1[i]);
-    s += t;
-    sa += fabs(t);
+    q.add(t);
+    qa.add(fabs(t));
   }
-  const T s2 = block_sum(s, red);
-  const T a2 = rtol > 0 ? block_sum(sa, red) : T(0);
+  const T s2 = block_value(q, red);
+  const T a2 = rtol > 0 ? block_value(qa, red) : T(0);
   if (rtol > 0 && (fabs(s1) <= T(rtol) * a1 || fabs(s2) <= T(rtol) * a2)) return;
   for (int i = threadIdx.x; i < N; i += blockDim.x) x[i] = x[i] * s1 / s2;
   __syncthreads();
 }
 
-// Last block of a member to finish reduces that member's partials in a
-// fixed order (deterministic), then re-arms the counter.
-static __device__ bool last_block_of_member(unsigned* counters, int member, int nitems, unsigned* flag) {
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const unsigned prev = atomicAdd(&counters[member], 1u);
-    *flag = (prev == (unsigned)(nitems - 1)) ? 1u : 0u;
-  }
-  __syncthreads();
-  const bool last = *flag != 0;
-  if (last) __threadfence();
-  return last;
-}
-
-static __device__ void reduce_member_partials2(const double* partials, int b, int n, double* out,
-                                        double* red) {
-  for (int k = 0; k < 2; ++k) {
-    double s = 0;
-    for (int q = (int)threadIdx.x; q < n; q += blockDim.x) s += __ldcg(&partials[2 * (size_t)(b + q) + k]);
-    out[k] = block_sum(s, red);
-  }
-}
-
 // --------------------------------------------------------- stage kernel
 
+template <typename T>
+struct StageOcc {
+  static constexpr int kMinBlocks = sizeof(T) == 4 ? 4 : 2;
+};
+
 template <typename T, int PASS, int ADV>
-__global__ void __launch_bounds__(kThreads)
-    stage_kernel(const MemberDev<T>* __restrict__ mems, const WorkItem* __restrict__ wl,
-                 StageArgs a, int staging_words, int max_n) {
+__global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
+    stage_kernel(const MemberDev<T>* __restrict__ mems, const WorkItem* __restrict__ wl, StageArgs a,
+                 int staging_words, int max_n) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* staging = reinterpret_cast<T*>(smem_raw);
   T* rows = staging + staging_words;  // 3 * max_n (row tasks)
   T* coefs = rows + 3 * max_n;        // kMaxKeep
-  T* redT = coefs + kMaxKeep;         // 32
-  double* redD = reinterpret_cast<double*>(redT + 32);  // 32
-  __shared__ unsigned last_flag;
+  T* redT = coefs + kMaxKeep;         // 64
+  __shared__ MemberDev<T> smd;
 
   const WorkItem w = wl[blockIdx.x];
-  const MemberDev<T>& md = mems[w.member];
+  load_member(mems, w.member, &smd);
+  const MemberDev<T>& md = smd;
   const int N = md.N, M = md.M, Mh = md.Mh;
   const T* gd_in = md.st[a.in_slot][F_GD];
   const T* iu_in = md.st[a.in_slot][F_IU];
@@ -418,22 +487,65 @@ __global__ void __launch_bounds__(kThreads)
   const double hstep = md.pcdt[PASS] * a.h_scale;
   Emit<T> em(md, a, T(hstep));
   const T ub_lon = T(a.ub_lon), ub_lat = T(a.ub_lat);
+  const bool plain_ops = a.taccum < 0 && a.tadd < 0 && a.tadd2 < 0;
+  // u, v supplied with this level (initial condition, diffusion): used as
+  // given, as the reference's space_operators reads state%u / state%v.
+  const bool given = a.uvslot && a.uvslot[w.member] == a.in_slot;
+  if (a.uvslot && a.out_slot >= 0 && threadIdx.x == 0 && a.uvslot[w.member] == a.out_slot)
+    a.uvslot[w.member] = -1;  // level overwritten: u, v derived from now on
 
   if (w.kind == 0) {
     // ---------------- bulk tile: rows j0..j0+R-1 are ordinary rows
     TileSmem<T> t = carve_tile(staging, w.rows, w.cols, w.j0, w.i0);
-    stage_tile(md, gd_in, iu_in, iv_in, t);
+    tile_issue(md, gd_in, iu_in, iv_in, t, given);
+    // While the tile is in flight, fetch the per-point update operands.
     const int npts = w.rows * w.cols;
-    for (int q = threadIdx.x; q < npts; q += blockDim.x) {
+    const bool base_in_tile = a.out_slot >= 0 && a.base_slot == a.in_slot;
+    T pre_b[kPPT][3], pre_p[kPPT][3];
+#pragma unroll
+    for (int k = 0; k < kPPT; ++k) {
+      const int q = threadIdx.x + k * kThreads;
+#pragma unroll
+      for (int f = 0; f < 3; ++f) {
+        pre_b[k][f] = T(0);
+        pre_p[k][f] = T(0);
+      }
+      if (q < npts) {
+        const int r = q / w.cols, c = q - r * w.cols;
+        const size_t o = (size_t)(w.j0 + r) * N + (w.i0 + c);
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+          if (a.out_slot >= 0 && !base_in_tile) pre_b[k][f] = md.st[a.base_slot][f][o];
+          if (a.do_ip) pre_p[k][f] = a.beta_mode == 0 ? md.td[a.tprev][f][o] : md.st[a.ip_slot][f][o];
+        }
+      }
+    }
+    tile_derive(md, t, false, given);
+#pragma unroll
+    for (int k = 0; k < kPPT; ++k) {
+      const int q = threadIdx.x + k * kThreads;
+      if (q >= npts) break;
       const int r = q / w.cols, c = q - r * w.cols;
       const int j = w.j0 + r, i = w.i0 + c;
       const int p = (r + 1) * t.SW + (c + 1);
+      const size_t o = (size_t)j * N + i;
+      if (base_in_tile) {
+        pre_b[k][F_GD] = t.gd[p];
+        pre_b[k][F_IU] = t.iu[p];
+        pre_b[k][F_IV] = t.iv[p];
+      }
       const T du = point_du<T, PASS, ADV>(md, t, j, p, ub_lon, ub_lat);
       const T dv = point_dv<T, PASS, ADV>(md, t, j, p, ub_lon, ub_lat);
       const T dg = point_dgd<T, PASS>(md, t, j, p);
-      em.put(F_IU, j, i, du, cf(md, CF_COS, j));
-      em.put(F_IV, j, i, dv, ch(md, CH_COS, j));
-      em.put(F_GD, j, i, dg, cf(md, CF_COS, j));
+      if (plain_ops) {
+        em.put(F_IU, o, du, cf(md, CF_COS, j), pre_b[k][F_IU], pre_p[k][F_IU]);
+        em.put(F_IV, o, dv, ch(md, CH_COS, j), pre_b[k][F_IV], pre_p[k][F_IV]);
+        em.put(F_GD, o, dg, cf(md, CF_COS, j), pre_b[k][F_GD], pre_p[k][F_GD]);
+      } else {
+        em.put(F_IU, o, du, cf(md, CF_COS, j), em.base_of(F_IU, o), em.prev_of(F_IU, o));
+        em.put(F_IV, o, dv, ch(md, CH_COS, j), em.base_of(F_IV, o), em.prev_of(F_IV, o));
+        em.put(F_GD, o, dg, cf(md, CF_COS, j), em.base_of(F_GD, o), em.prev_of(F_GD, o));
+      }
     }
   } else {
     // ---------------- whole-row task: row index j (full row j, half row j)
@@ -445,12 +557,13 @@ __global__ void __launch_bounds__(kThreads)
     T* rdu = rows;
     T* rdv = rows + max_n;
     T* rdg = rows + 2 * max_n;
-    double cap = 0;
+    Acc<double> cap;
     for (int c0 = 0; c0 < N; c0 += kRowChunk) {
       const int W = min(kRowChunk, N - c0);
       TileSmem<T> t = carve_tile(staging, 1, W, j, c0);
       __syncthreads();
-      stage_tile(md, gd_in, iu_in, iv_in, t);
+      tile_issue(md, gd_in, iu_in, iv_in, t, given);
+      tile_derive(md, t, false, given);
       for (int c = threadIdx.x; c < W; c += blockDim.x) {
         const int p = t.SW + (c + 1);
         const int i = c0 + c;
@@ -458,12 +571,12 @@ __global__ void __launch_bounds__(kThreads)
         rdv[i] = has_dv ? point_dv<T, PASS, ADV>(md, t, j, p, ub_lon, ub_lat) : T(0);
         if (south || north) {
           // src/dycore_mod.F90:572-596: sp += (ig(j)+ig(j+1)) iv(j);
-          // np -= (ig(j)+ig(j-1)) iv(j-1).  Accumulated in FP64.
+          // np -= (ig(j)+ig(j-1)) iv(j-1).  Terms and sum in FP64.
           if (PASS != kSlowPass) {
             if (south)
-              cap += ((double)t.ig[p] + (double)t.ig[p + t.SW]) * (double)t.iv[p];
+              cap.add(((double)t.ig[p] + (double)t.ig[p + t.SW]) * (double)t.iv[p]);
             else
-              cap += ((double)t.ig[p] + (double)t.ig[p - t.SW]) * (double)t.iv[p - t.SW];
+              cap.add(((double)t.ig[p] + (double)t.ig[p - t.SW]) * (double)t.iv[p - t.SW]);
           }
           rdg[i] = T(0);
         } else {
@@ -473,7 +586,8 @@ __global__ void __launch_bounds__(kThreads)
     }
     __syncthreads();
     if ((south || north) && PASS != kSlowPass) {
-      double s = block_sum(cap, redD);
+      double* redD = reinterpret_cast<double*>(redT + 64);
+      double s = block_value(cap, redD);
       if (north) s = -s;
       s = s * 2.0 / N / kRadius / (kPi / Mh);
       // dgd = - mass_div_lon - mass_div_lat with mass_div_lon = 0 at poles
@@ -491,37 +605,55 @@ __global__ void __launch_bounds__(kThreads)
     const T cj = cf(md, CF_COS, j);
     const T chj = has_dv ? ch(md, CH_COS, j) : T(0);
     for (int i = threadIdx.x; i < N; i += blockDim.x) {
+      const size_t o = ro + i;
       // du is 0 on pole rows (never assigned by the reference); inner
       // products skip pole-row du (src/types_mod.F90:355).
       if (has_du)
-        em.put(F_IU, j, i, rdu[i], cj);
+        em.put(F_IU, o, rdu[i], cj, em.base_of(F_IU, o), em.prev_of(F_IU, o));
       else
-        em.put(F_IU, j, i, T(0), T(0));
-      if (has_dv) em.put(F_IV, j, i, rdv[i], chj);
-      em.put(F_GD, j, i, rdg[i], cj);
+        em.put(F_IU, o, T(0), T(0), em.base_of(F_IU, o), T(0));
+      if (has_dv) em.put(F_IV, o, rdv[i], chj, em.base_of(F_IV, o), em.prev_of(F_IV, o));
+      em.put(F_GD, o, rdg[i], cj, em.base_of(F_GD, o), em.prev_of(F_GD, o));
     }
   }
 
   if (a.do_ip) {
-    // Per-item partials, then the member's last block forms beta
-    // (src/dycore_mod.F90:784-786; isp: :743-746).
-    const double s1 = block_sum((double)em.ip1, redD);
-    const double s2 = block_sum((double)em.ip2, redD);
+    // Per-item partials of the inner products (src/dycore_mod.F90:784-785;
+    // isp :743-744); beta_kernel reduces them per member.  FP64 reduces in
+    // double-double, FP32 in FP32 (FP64 arithmetic is the scarce unit).
+    const Acc<T> s1 = block_acc(em.ip1, redT);
+    const Acc<T> s2 = block_acc(em.ip2, redT);
     if (threadIdx.x == 0) {
-      a.partials[2 * (size_t)w.pidx] = s1;
-      a.partials[2 * (size_t)w.pidx + 1] = s2;
+      double* pp = a.partials + 4 * (size_t)w.pidx;
+      pp[0] = (double)s1.s;
+      pp[1] = (double)s1.c;
+      pp[2] = (double)s2.s;
+      pp[3] = (double)s2.c;
     }
-    if (last_block_of_member(a.counters, w.member, md.pcount, &last_flag)) {
-      double tot[2];
-      reduce_member_partials2(a.partials, md.pbase, md.pcount, tot, redD);
-      if (threadIdx.x == 0) {
-        const double ip1 = tot[0], ip2 = tot[1];
-        double beta = (a.qcon && ip1 != 0.0 && ip2 != 0.0) ? ip1 / ip2 : 1.0;
-        if (a.beta_mode == 1) beta = beta * 4.0 / md.dt;
-        a.beta[w.member] = beta;
-        a.counters[w.member] = 0;
-      }
-    }
+  }
+}
+
+// beta of predict_correct (src/dycore_mod.F90:784-786) or isp (:743-746),
+// one block per member over that member's partials.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    beta_kernel(const MemberDev<T>* __restrict__ mems, const int* __restrict__ slots, const double* partials,
+                double* beta, int qcon, int beta_mode) {
+  __shared__ double red[64];
+  const int s = slots[blockIdx.x];
+  const MemberDev<T>& md = mems[s];
+  Acc<double> a1, a2;
+  for (int q = threadIdx.x; q < md.pcount; q += blockDim.x) {
+    const double* pp = partials + 4 * (size_t)(md.pbase + q);
+    a1.merge(pp[0], pp[1]);
+    a2.merge(pp[2], pp[3]);
+  }
+  const double ip1 = block_value(a1, red);
+  const double ip2 = block_value(a2, red);
+  if (threadIdx.x == 0) {
+    double b = (qcon && ip1 != 0.0 && ip2 != 0.0) ? ip1 / ip2 : 1.0;
+    if (beta_mode == 1) b = b * 4.0 / md.dt;
+    beta[s] = b;
   }
 }
 
@@ -531,8 +663,7 @@ __global__ void __launch_bounds__(kThreads)
 // levels carry a compensation word: new = (hi + lo) + dt*T via TwoSum.
 
 template <typename T>
-__device__ inline void final_point(const MemberDev<T>& md, const FinalArgs& a, int f, size_t o,
-                                   double hstep) {
+__device__ inline void final_point(const MemberDev<T>& md, const FinalArgs& a, int f, size_t o, double hstep) {
   const T tv = md.td[a.tslot][f][o];
   const T hi = md.st[a.base_slot][f][o];
   if (a.use_lo) {
@@ -550,13 +681,16 @@ __device__ inline void final_point(const MemberDev<T>& md, const FinalArgs& a, i
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-    final_kernel(const MemberDev<T>* __restrict__ mems, const WorkItem* __restrict__ wl,
-                 FinalArgs a) {
+    final_kernel(const MemberDev<T>* __restrict__ mems, const WorkItem* __restrict__ wl, FinalArgs a) {
+  __shared__ MemberDev<T> smd;
   const WorkItem w = wl[blockIdx.x];
-  const MemberDev<T>& md = mems[w.member];
+  load_member(mems, w.member, &smd);
+  const MemberDev<T>& md = smd;
   const int N = md.N, Mh = md.Mh;
   double hstep = md.pcdt[a.pass] * a.h_scale;
   if (a.beta) hstep = md.pcdt[a.pass] * a.h_scale * a.beta[w.member];
+  // This level's u, v are derived from its new state from now on.
+  if (a.uvslot && threadIdx.x == 0 && a.uvslot[w.member] == a.out_slot) a.uvslot[w.member] = -1;
   if (w.kind == 0) {
     const int npts = w.rows * w.cols;
     for (int q = threadIdx.x; q < npts; q += blockDim.x) {
@@ -589,30 +723,30 @@ __device__ inline double val64(const MemberDev<T>& md, int slot, int f, size_t o
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-    diag_kernel(const MemberDev<T>* __restrict__ mems, const WorkItem* __restrict__ wl,
-                DiagArgs a) {
-  __shared__ double red[32];
-  __shared__ unsigned last_flag;
+    diag_kernel(const MemberDev<T>* __restrict__ mems, const WorkItem* __restrict__ wl, DiagArgs a) {
+  __shared__ double red[64];
+  __shared__ MemberDev<T> smd;
   const WorkItem w = wl[blockIdx.x];
-  const MemberDev<T>& md = mems[w.member];
+  load_member(mems, w.member, &smd);
+  const MemberDev<T>& md = smd;
   const int N = md.N, M = md.M, Mh = md.Mh;
   const double* dc = md.dcoef;
-  double mass = 0, en = 0;
+  Acc<double> mass, en;
   auto point = [&](int j, int i, bool hv) {
     const size_t o = (size_t)j * N + i;
     const double g = val64(md, a.slot, F_GD, o);
     const double gh = (double)md.ghs[o];
-    mass = mass + dc[j] * g;
+    mass.add(dc[j] * g);
     if (j >= 1 && j <= M - 2) {
       const double uu = val64(md, a.slot, F_IU, o);
-      en = en + uu * uu * dc[M + j];
+      en.add(uu * uu * dc[M + j]);
     }
     if (hv) {
       const double vv = val64(md, a.slot, F_IV, o);
-      en = en + vv * vv * dc[2 * M + j];
+      en.add(vv * vv * dc[2 * M + j]);
     }
     const double hh = g + gh;
-    en = en + hh * hh * dc[M + j];
+    en.add(hh * hh * dc[M + j]);
   };
   if (w.kind == 0) {
     const int npts = w.rows * w.cols;
@@ -623,27 +757,39 @@ __global__ void __launch_bounds__(kThreads)
   } else {
     for (int i = threadIdx.x; i < N; i += blockDim.x) point(w.j0, i, w.j0 <= Mh - 1);
   }
-  const double sm = block_sum(mass, red);
-  const double se = block_sum(en, red);
+  const Acc<double> sm = block_acc(mass, red);
+  const Acc<double> se = block_acc(en, red);
   if (threadIdx.x == 0) {
-    a.partials[2 * (size_t)w.pidx] = sm;
-    a.partials[2 * (size_t)w.pidx + 1] = se;
+    double* pp = a.partials + 4 * (size_t)w.pidx;
+    pp[0] = sm.s;
+    pp[1] = sm.c;
+    pp[2] = se.s;
+    pp[3] = se.c;
   }
-  if (last_block_of_member(a.counters, w.member, md.pcount, &last_flag)) {
-    double tot[2];
-    reduce_member_partials2(a.partials, md.pbase, md.pcount, tot, red);
-    if (threadIdx.x == 0) {
-      const double total_mass = tot[0] * (kRadius * kRadius);
-      const double total_energy = tot[1];
-      a.diag[3 * w.member] = total_mass;
-      a.diag[3 * w.member + 1] = total_energy;
-      a.diag[3 * w.member + 2] = a.beta ? a.beta[w.member] : 1.0;
-      const long long step = a.steps[w.member] + 1;
-      a.steps[w.member] = step;
-      if ((isnan(total_mass) || isnan(total_energy)) && a.nan_step[w.member] < 0)
-        a.nan_step[w.member] = step;
-      a.counters[w.member] = 0;
-    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    diag_finalize_kernel(const MemberDev<T>* __restrict__ mems, const int* __restrict__ slots, DiagArgs a) {
+  __shared__ double red[64];
+  const int s = slots[blockIdx.x];
+  const MemberDev<T>& md = mems[s];
+  Acc<double> m, e;
+  for (int q = threadIdx.x; q < md.pcount; q += blockDim.x) {
+    const double* pp = a.partials + 4 * (size_t)(md.pbase + q);
+    m.merge(pp[0], pp[1]);
+    e.merge(pp[2], pp[3]);
+  }
+  const double tm = block_value(m, red);
+  const double te = block_value(e, red);
+  if (threadIdx.x == 0) {
+    const double total_mass = tm * (kRadius * kRadius);
+    a.diag[3 * s] = total_mass;
+    a.diag[3 * s + 1] = te;
+    a.diag[3 * s + 2] = a.beta ? a.beta[s] : 1.0;
+    const long long step = a.steps[s] + (a.count_step ? 1 : 0);
+    a.steps[s] = step;
+    if ((isnan(total_mass) || isnan(te)) && a.nan_step[s] < 0) a.nan_step[s] = step;
   }
 }
 
@@ -660,14 +806,13 @@ __device__ inline T lap_lon(const T* f, int p, T d) {
 }
 
 template <typename T>
-__device__ inline T point_gdd_like(const MemberDev<T>& md, const TileSmem<T>& t, const T* f, int j,
-                                   int p) {
+__device__ inline T point_gdd_like(const MemberDev<T>& md, const TileSmem<T>& t, const T* f, int j, int p) {
   // src/diffusion_mod.F90:109-115 (and :135-143 for u)
   const int SW = t.SW;
   const T dl = cf(md, CF_DLAT, j);
   return lap_lon(f, p, cf(md, CF_DLON, j)) +
-         ((f[p + SW] - f[p]) * ch(md, CH_COS, j) - (f[p] - f[p - SW]) * ch(md, CH_COS, j - 1)) /
-             (dl * dl) * cf(md, CF_COS, j);
+         ((f[p + SW] - f[p]) * ch(md, CH_COS, j) - (f[p] - f[p - SW]) * ch(md, CH_COS, j - 1)) / (dl * dl) *
+             cf(md, CF_COS, j);
 }
 
 template <typename T>
@@ -678,8 +823,8 @@ __device__ inline T point_vd(const MemberDev<T>& md, const TileSmem<T>& t, int j
   T vd = lap_lon(v, p, ch(md, CH_DLON, jh));
   const T dl = ch(md, CH_DLAT, jh);
   if (jh >= 1 && jh <= Mh - 2) {
-    vd = vd + ((v[p + SW] - v[p]) * cf(md, CF_COS, jh + 1) - (v[p] - v[p - SW]) * cf(md, CF_COS, jh)) /
-                  (dl * dl) * ch(md, CH_COS, jh);
+    vd = vd + ((v[p + SW] - v[p]) * cf(md, CF_COS, jh + 1) - (v[p] - v[p - SW]) * cf(md, CF_COS, jh)) / (dl * dl) *
+                  ch(md, CH_COS, jh);
   } else if (jh == 0) {
     vd = vd + (v[p + SW] - v[p]) * cf(md, CF_COS, jh + 1) / (dl * dl) * ch(md, CH_COS, jh);
   } else {
@@ -690,15 +835,18 @@ __device__ inline T point_vd(const MemberDev<T>& md, const TileSmem<T>& t, int j
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-    diffusion_lap_kernel(const MemberDev<T>* __restrict__ mems, const WorkItem* __restrict__ wl,
-                         int slot, double c, int staging_words, int max_n) {
+    diffusion_lap_kernel(const MemberDev<T>* __restrict__ mems, const WorkItem* __restrict__ wl, int slot, double c,
+                         int staging_words, int max_n) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* staging = reinterpret_cast<T*>(smem_raw);
   T* rows = staging + staging_words;
   T* coefs = rows + 3 * max_n;
-  double* redD = reinterpret_cast<double*>(coefs + kMaxKeep + 32);
+  T* redT = coefs + kMaxKeep;
+  double* redD = reinterpret_cast<double*>(redT + 64);
+  __shared__ MemberDev<T> smd;
   const WorkItem w = wl[blockIdx.x];
-  const MemberDev<T>& md = mems[w.member];
+  load_member(mems, w.member, &smd);
+  const MemberDev<T>& md = smd;
   const int N = md.N, M = md.M, Mh = md.Mh;
   const T* gd_in = md.st[slot][F_GD];
   T* go = md.st[SL_SA][F_GD];
@@ -707,7 +855,8 @@ __global__ void __launch_bounds__(kThreads)
   const T cc_ = T(c);
   if (w.kind == 0) {
     TileSmem<T> t = carve_tile(staging, w.rows, w.cols, w.j0, w.i0);
-    stage_tile(md, gd_in, md.st[slot][F_IU], md.st[slot][F_IV], t, true);
+    tile_issue(md, gd_in, md.st[slot][F_IU], md.st[slot][F_IV], t);
+    tile_derive(md, t, true);
     const int npts = w.rows * w.cols;
     for (int q = threadIdx.x; q < npts; q += blockDim.x) {
       const int r = q / w.cols, cl = q - r * w.cols;
@@ -727,22 +876,26 @@ __global__ void __launch_bounds__(kThreads)
     T* rg = rows;
     T* ru = rows + max_n;
     T* rv = rows + 2 * max_n;
-    T* rg0 = nullptr;
-    double cap = 0;
+    Acc<double> cap;
     for (int c0 = 0; c0 < N; c0 += kRowChunk) {
       const int W = min(kRowChunk, N - c0);
       TileSmem<T> t = carve_tile(staging, 1, W, j, c0);
       __syncthreads();
-      stage_tile(md, gd_in, md.st[slot][F_IU], md.st[slot][F_IV], t, true);
+      tile_issue(md, gd_in, md.st[slot][F_IU], md.st[slot][F_IV], t);
+      tile_derive(md, t, true);
       for (int cl = threadIdx.x; cl < W; cl += blockDim.x) {
         const int p = t.SW + (cl + 1);
         const int i = c0 + cl;
         if (pole) {
-          // sp = sp + gd(i,j+1) - gd(i,j); np = np - (gd(i,j) - gd(i,j-1))
-          if (j == 0)
-            cap += (double)t.gd[p + t.SW] - (double)t.gd[p];
-          else
-            cap -= (double)t.gd[p] - (double)t.gd[p - t.SW];
+          // sp = sp + gd(i,j+1) - gd(i,j); np = np - (gd(i,j) - gd(i,j-1)):
+          // the terms +gd(j+1), -gd(j) (south) and -gd(j), +gd(j-1) (north).
+          if (j == 0) {
+            cap.add((double)t.gd[p + t.SW]);
+            cap.add(-(double)t.gd[p]);
+          } else {
+            cap.add(-(double)t.gd[p]);
+            cap.add((double)t.gd[p - t.SW]);
+          }
           rg[i] = T(0);
         } else {
           rg[i] = point_gdd_like(md, t, t.gd, j, p);
@@ -757,14 +910,13 @@ __global__ void __launch_bounds__(kThreads)
     }
     __syncthreads();
     if (pole) {
-      const double s = block_sum(cap, redD);
+      const double s = block_value(cap, redD);
       const int jh = (j == 0) ? 0 : Mh - 1;
       const double dl = (double)cf(md, CF_DLAT, j);
       const double val = s * (double)ch(md, CH_COS, jh) / (dl * dl) * (double)cf(md, CF_COS, j) / N;
       for (int i = threadIdx.x; i < N; i += blockDim.x) rg[i] = T(val);
       __syncthreads();
     }
-    (void)rg0;
     if (has_u && (info & RI_FLAG_FULL)) {
       filter_project(md, rg, ri_keep_full(info), coefs);
       filter_project(md, ru, ri_keep_full(info), coefs);
@@ -783,10 +935,12 @@ __global__ void __launch_bounds__(kThreads)
 // iap_transform (src/types_mod.F90:399-426) of SA = (gd', u', v') into slot.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-    diffusion_iap_kernel(const MemberDev<T>* __restrict__ mems, const WorkItem* __restrict__ wl,
-                         int slot) {
+    diffusion_iap_kernel(const MemberDev<T>* __restrict__ mems, const WorkItem* __restrict__ wl, int slot,
+                         int* uvslot) {
+  __shared__ MemberDev<T> smd;
   const WorkItem w = wl[blockIdx.x];
-  const MemberDev<T>& md = mems[w.member];
+  load_member(mems, w.member, &smd);
+  const MemberDev<T>& md = smd;
   const int N = md.N, Mh = md.Mh;
   const T* g = md.st[SL_SA][F_GD];
   const T* u = md.st[SL_SA][F_IU];
@@ -798,6 +952,9 @@ __global__ void __launch_bounds__(kThreads)
     md.st[slot][F_GD][o] = g[o];
     md.st[slot][F_IU][o] = T(0.5) * (ig + sqrt(g[(size_t)j * N + ip])) * u[o];
     if (hv) md.st[slot][F_IV][o] = T(0.5) * (ig + sqrt(g[o + N])) * v[o];
+    // The next step's first stage reads the diffused u, v themselves.
+    md.given_u[o] = u[o];
+    if (hv) md.given_v[o] = v[o];
     if (md.lo[slot][F_GD]) {
       md.lo[slot][F_GD][o] = T(0);
       md.lo[slot][F_IU][o] = T(0);
@@ -813,16 +970,18 @@ __global__ void __launch_bounds__(kThreads)
   } else {
     for (int i = threadIdx.x; i < N; i += blockDim.x) point(w.j0, i, w.j0 <= Mh - 1);
   }
+  if (uvslot && threadIdx.x == 0) uvslot[w.member] = slot;
 }
 
 // copy_data(state1, state2) (src/types_mod.F90:229-241) of the prognostic
 // words, compensation included.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-    copy_state_kernel(const MemberDev<T>* __restrict__ mems, const WorkItem* __restrict__ wl,
-                      int from, int to) {
+    copy_state_kernel(const MemberDev<T>* __restrict__ mems, const WorkItem* __restrict__ wl, int from, int to) {
+  __shared__ MemberDev<T> smd;
   const WorkItem w = wl[blockIdx.x];
-  const MemberDev<T>& md = mems[w.member];
+  load_member(mems, w.member, &smd);
+  const MemberDev<T>& md = smd;
   const int N = md.N, Mh = md.Mh;
   auto point = [&](int j, int i, bool hv) {
     const size_t o = (size_t)j * N + i;
@@ -863,19 +1022,19 @@ size_t stage_smem_bytes(int tile_rows, int tile_cols, int max_n, int* staging_wo
   const int sw = ((bulk > row ? bulk : row) + 3) & ~3;
   max_n = (max_n + 1) & ~1;
   if (staging_words) *staging_words = sw;
-  return (size_t)(sw + 3 * max_n + kMaxKeep + 32) * sizeof(T) + 32 * sizeof(double) + 16;
+  return (size_t)(sw + 3 * max_n + kMaxKeep + 64) * sizeof(T) + 64 * sizeof(double) + 16;
 }
 
 template <typename T, int PASS, int ADV>
-static int launch_stage_t(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int tile_rows,
-                          int tile_cols, int max_n, const StageArgs& a, cudaStream_t s) {
+static int launch_stage_t(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int tile_rows, int tile_cols,
+                          int max_n, const StageArgs& a, cudaStream_t s) {
   int sw = 0;
   max_n = (max_n + 1) & ~1;
   const size_t smem = stage_smem_bytes<T>(tile_rows, tile_cols, max_n, &sw);
   static size_t configured = 0;
   if (smem > configured) {
-    if (cudaFuncSetAttribute(stage_kernel<T, PASS, ADV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem) != cudaSuccess)
+    if (cudaFuncSetAttribute(stage_kernel<T, PASS, ADV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
       return check_launch();
     configured = smem;
   }
@@ -884,9 +1043,10 @@ static int launch_stage_t(const MemberDev<T>* mem, const WorkItem* wl, int nwork
 }
 
 template <typename T>
-int launch_stage(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int adv, int tile_rows,
-                 int tile_cols, int max_n, const StageArgs& a, void* stream) {
+int launch_stage(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int adv, int tile_rows, int tile_cols,
+                 int max_n, const StageArgs& a, void* stream) {
   if (nwork <= 0) return GDC_OK;
+  if (tile_rows * tile_cols > kPPT * kThreads) return GDC_E_CONFIG;
   cudaStream_t s = (cudaStream_t)stream;
 #define GDC_DISPATCH(P, A) \
   if (a.pass == P && adv == A) return launch_stage_t<T, P, A>(mem, wl, nwork, tile_rows, tile_cols, max_n, a, s);
@@ -901,24 +1061,34 @@ int launch_stage(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int adv
 }
 
 template <typename T>
-int launch_final(const MemberDev<T>* mem, const WorkItem* wl, int nwork, const FinalArgs& a,
-                 void* stream) {
+int launch_beta(const MemberDev<T>* mem, const int* slots, int nmembers, const double* partials, double* beta,
+                int qcon, int beta_mode, void* stream) {
+  if (nmembers <= 0) return GDC_OK;
+  beta_kernel<T><<<nmembers, kThreads, 0, (cudaStream_t)stream>>>(mem, slots, partials, beta, qcon, beta_mode);
+  return check_launch();
+}
+
+template <typename T>
+int launch_final(const MemberDev<T>* mem, const WorkItem* wl, int nwork, const FinalArgs& a, void* stream) {
   if (nwork <= 0) return GDC_OK;
   final_kernel<T><<<nwork, kThreads, 0, (cudaStream_t)stream>>>(mem, wl, a);
   return check_launch();
 }
 
 template <typename T>
-int launch_diag(const MemberDev<T>* mem, const WorkItem* wl, int nwork, const DiagArgs& a,
-                void* stream) {
+int launch_diag(const MemberDev<T>* mem, const WorkItem* wl, int nwork, const int* slots, int nmembers,
+                const DiagArgs& a, void* stream) {
   if (nwork <= 0) return GDC_OK;
   diag_kernel<T><<<nwork, kThreads, 0, (cudaStream_t)stream>>>(mem, wl, a);
+  int rc = check_launch();
+  if (rc) return rc;
+  diag_finalize_kernel<T><<<nmembers, kThreads, 0, (cudaStream_t)stream>>>(mem, slots, a);
   return check_launch();
 }
 
 template <typename T>
-int launch_diffusion(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int tile_rows,
-                     int tile_cols, int max_n, int slot, double sign_dt_coef, void* stream) {
+int launch_diffusion(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int tile_rows, int tile_cols,
+                     int max_n, int slot, double sign_dt_coef, int* uvslot, void* stream) {
   if (nwork <= 0) return GDC_OK;
   cudaStream_t s = (cudaStream_t)stream;
   int sw = 0;
@@ -926,21 +1096,21 @@ int launch_diffusion(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int
   const size_t smem = stage_smem_bytes<T>(tile_rows, tile_cols, max_n, &sw);
   static size_t configured = 0;
   if (smem > configured) {
-    if (cudaFuncSetAttribute(diffusion_lap_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem) != cudaSuccess)
+    if (cudaFuncSetAttribute(diffusion_lap_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
       return check_launch();
     configured = smem;
   }
   diffusion_lap_kernel<T><<<nwork, kThreads, smem, s>>>(mem, wl, slot, sign_dt_coef, sw, max_n);
   int rc = check_launch();
   if (rc != GDC_OK) return rc;
-  diffusion_iap_kernel<T><<<nwork, kThreads, 0, s>>>(mem, wl, slot);
+  diffusion_iap_kernel<T><<<nwork, kThreads, 0, s>>>(mem, wl, slot, uvslot);
   return check_launch();
 }
 
 template <typename T>
-int launch_copy_state(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int from_slot,
-                      int to_slot, void* stream) {
+int launch_copy_state(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int from_slot, int to_slot,
+                      void* stream) {
   if (nwork <= 0) return GDC_OK;
   copy_state_kernel<T><<<nwork, kThreads, 0, (cudaStream_t)stream>>>(mem, wl, from_slot, to_slot);
   return check_launch();

@@ -5,11 +5,12 @@
 namespace gdc {
 
 template size_t stage_smem_bytes<float>(int, int, int, int*);
-template int launch_diffusion<float>(const MemberDev<float>*, const WorkItem*, int, int, int, int, int, double, void*);
+template int launch_diffusion<float>(const MemberDev<float>*, const WorkItem*, int, int, int, int, int, double, int*, void*);
 template int launch_copy_state<float>(const MemberDev<float>*, const WorkItem*, int, int, int, void*);
 template int launch_stage<float>(const MemberDev<float>*, const WorkItem*, int, int, int, int, int,
                                  const StageArgs&, void*);
 template int launch_final<float>(const MemberDev<float>*, const WorkItem*, int, const FinalArgs&, void*);
-template int launch_diag<float>(const MemberDev<float>*, const WorkItem*, int, const DiagArgs&, void*);
+template int launch_diag<float>(const MemberDev<float>*, const WorkItem*, int, const int*, int, const DiagArgs&, void*);
+template int launch_beta<float>(const MemberDev<float>*, const int*, int, const double*, double*, int, int, void*);
 
 }  // namespace gdc

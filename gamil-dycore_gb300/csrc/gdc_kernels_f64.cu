@@ -8,11 +8,12 @@
 namespace gdc {
 
 template size_t stage_smem_bytes<double>(int, int, int, int*);
-template int launch_diffusion<double>(const MemberDev<double>*, const WorkItem*, int, int, int, int, int, double, void*);
+template int launch_diffusion<double>(const MemberDev<double>*, const WorkItem*, int, int, int, int, int, double, int*, void*);
 template int launch_copy_state<double>(const MemberDev<double>*, const WorkItem*, int, int, int, void*);
 template int launch_stage<double>(const MemberDev<double>*, const WorkItem*, int, int, int, int, int,
                                   const StageArgs&, void*);
 template int launch_final<double>(const MemberDev<double>*, const WorkItem*, int, const FinalArgs&, void*);
-template int launch_diag<double>(const MemberDev<double>*, const WorkItem*, int, const DiagArgs&, void*);
+template int launch_diag<double>(const MemberDev<double>*, const WorkItem*, int, const int*, int, const DiagArgs&, void*);
+template int launch_beta<double>(const MemberDev<double>*, const int*, int, const double*, double*, int, int, void*);
 
 }  // namespace gdc

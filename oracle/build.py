@@ -16,15 +16,23 @@ HERE = Path(__file__).resolve().parent
 OUT = HERE / "_build"
 SRC = HERE / "gdc_oracle.c"
 LIB = OUT / "libgdc_oracle.so"
+# Timing variant for the CPU baseline: plain running sums, compiled with the
+# reference's own optimisation flags (-Ofast, CMakeLists.txt:13).  Never
+# used as a checker.
+LIB_FAST = OUT / "libgdc_oracle_fast.so"
+
+
+def _compile(out: Path, flags: list[str], force: bool) -> None:
+    newest = max(SRC.stat().st_mtime, (HERE / "gdc_oracle.h").stat().st_mtime)
+    if force or not out.exists() or out.stat().st_mtime < newest:
+        cmd = ["gcc", *flags, "-std=c99", "-fPIC", "-shared", "-o", str(out), str(SRC), "-lm"]
+        subprocess.run(cmd, check=True)
 
 
 def build(force: bool = False) -> Path:
     OUT.mkdir(exist_ok=True)
-    if force or not LIB.exists() or LIB.stat().st_mtime < max(SRC.stat().st_mtime,
-                                                               (HERE / "gdc_oracle.h").stat().st_mtime):
-        cmd = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-std=c99", "-fPIC", "-shared",
-               "-o", str(LIB), str(SRC), "-lm"]
-        subprocess.run(cmd, check=True)
+    _compile(LIB, ["-O2", "-ffp-contract=off", "-fno-fast-math"], force)
+    _compile(LIB_FAST, ["-Ofast", "-DGDO_PLAIN_SUMS"], force)
     return LIB
 
 

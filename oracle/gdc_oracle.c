@@ -12,6 +12,14 @@
  * (paths relative to the gamil-dycore project root).  Build with
  * -O2 -ffp-contract=off so that no FMA contraction or reassociation changes
  * the order of operations.
+ *
+ * Sums: the reference's reductions (filter s1/s2 and FFT coefficients, the
+ * pole caps, beta's inner products, the diagnostics) are evaluated as the
+ * correctly rounded sum of the same rounded terms (exact expansion
+ * arithmetic, Shewchuk 1997).  The reference's own summation order is not
+ * fixed -- it is built with -Ofast, which lets the compiler reassociate --
+ * and the correctly rounded sum is the order-independent value every
+ * order approximates; the CUDA path computes the same value.
  */
 #include "gdc_oracle.h"
 
@@ -82,6 +90,77 @@ struct gdo_model {
 #define AT(m, f, i, j) ((f)[((j) + 1) * (m)->NP + ((i) + 1)])
 
 static double* zalloc(size_t n) { return (double*)calloc(n, sizeof(double)); }
+
+/* ---- correctly rounded summation ------------------------------------
+ * A nonoverlapping expansion of increasing magnitude grown term by term
+ * with Knuth's TwoSum (zero components dropped), then rounded once to
+ * nearest-even (Shewchuk, "Adaptive Precision Floating-Point Arithmetic
+ * and Fast Robust Geometric Predicates", 1997). */
+typedef struct {
+  double p[80];
+  int n;
+  double special; /* running sum of infinities / NaNs */
+  int has_special;
+} xsum;
+
+static void xs_init(xsum* x) { x->n = 0; x->special = 0.0; x->has_special = 0; }
+
+#ifdef GDO_PLAIN_SUMS
+/* Timing build (the CPU baseline): the reference's plain running sums,
+ * compiled like the reference (-Ofast). */
+static void xs_add(xsum* x, double v) {
+  if (x->n == 0) {
+    x->p[0] = 0.0;
+    x->n = 1;
+  }
+  x->p[0] += v;
+}
+static double xs_value(const xsum* x) { return x->n ? x->p[0] : 0.0; }
+#else
+static void xs_add(xsum* x, double v) {
+  if (!isfinite(v)) {
+    x->special += v;
+    x->has_special = 1;
+    return;
+  }
+  int k = 0;
+  for (int q = 0; q < x->n; ++q) {
+    double y = x->p[q];
+    double hi = v + y;
+    double bp = hi - v;
+    double lo = (v - (hi - bp)) + (y - bp);
+    if (lo != 0.0) x->p[k++] = lo;
+    v = hi;
+  }
+  x->p[k++] = v;
+  x->n = k;
+}
+
+static double xs_value(const xsum* x) {
+  if (x->has_special) return x->special;
+  int n = x->n;
+  if (n == 0) return 0.0;
+  double hi = x->p[--n];
+  double lo = 0.0;
+  while (n > 0) {
+    double a = hi, b = x->p[--n];
+    hi = a + b;
+    double bv = hi - a;
+    lo = b - bv;
+    if (lo != 0.0) break;
+  }
+  /* Round-half-even correction: when the remainder is exactly half an ulp
+   * and the next component has the same sign, the true sum lies beyond
+   * the halfway point. */
+  if (n > 0 && ((lo < 0.0 && x->p[n - 1] < 0.0) || (lo > 0.0 && x->p[n - 1] > 0.0))) {
+    double b = lo * 2.0;
+    double a = hi + b;
+    double bv = a - hi;
+    if (b == bv) hi = a;
+  }
+  return hi;
+}
+#endif
 static size_t full_sz(const gdo_model* m) { return (size_t)(m->M + 4) * m->NP; }
 static size_t half_sz(const gdo_model* m) { return (size_t)(m->Mh + 4) * m->NP; }
 
@@ -241,6 +320,13 @@ gdo_model* gdo_create(int num_lon, int num_lat, double time_step_size,
 
 void gdo_set_rescale_rtol(gdo_model* m, double rtol) { m->rescale_rtol = rtol; }
 
+double gdo_fsum(const double* x, int n) {
+  xsum acc;
+  xs_init(&acc);
+  for (int k = 0; k < n; ++k) xs_add(&acc, x[k]);
+  return xs_value(&acc);
+}
+
 void gdo_destroy(gdo_model* m) {
   if (!m) return;
   double* bufs[] = {m->full_lat, m->half_lat, m->full_cos, m->half_cos,
@@ -275,18 +361,20 @@ static void filter_row(const gdo_model* m, const double* fac, double* x) {
   for (int i = 1; i <= N; ++i) local[i - 1] = x[i + 1];
   for (int p = 0; p < N; ++p) { /* p = packed index - 1 */
     if (fac[p] == 0.0) continue;
-    double s = 0.0;
+    xsum acc;
+    xs_init(&acc);
+    double s;
     if (p == 0) {
-      for (int n = 0; n < N; ++n) s = s + local[n];
-      s = s * (1.0 / N);
+      for (int n = 0; n < N; ++n) xs_add(&acc, local[n]);
+      s = xs_value(&acc) * (1.0 / N);
     } else if (N % 2 == 0 && p == N - 1) {
-      for (int n = 0; n < N; ++n) s = s + ((n & 1) ? -local[n] : local[n]);
-      s = s * (1.0 / N);
+      for (int n = 0; n < N; ++n) xs_add(&acc, (n & 1) ? -local[n] : local[n]);
+      s = xs_value(&acc) * (1.0 / N);
     } else {
       int k = (p + 1) / 2;
       const double* tab = (p % 2 == 1) ? m->ctab : m->stab;
-      for (int n = 0; n < N; ++n) s = s + local[n] * tab[(int)(((long)k * n) % N)];
-      s = s * (2.0 / N);
+      for (int n = 0; n < N; ++n) xs_add(&acc, local[n] * tab[(int)(((long)k * n) % N)]);
+      s = xs_value(&acc) * (2.0 / N);
     }
     coefs[p] = s * fac[p];
   }
@@ -475,17 +563,21 @@ static void mass_divergence(gdo_model* m, const state_t* s, tend_t* t) {
                         0.5 / m->full_dlat[j];
   {
     int j = 1;
-    double sp = 0.0;
+    xsum acc;
+    xs_init(&acc);
     for (int i = 1; i <= N; ++i)
-      sp = sp + (AT(m, s->ig, i, j) + AT(m, s->ig, i, j + 1)) * AT(m, s->iv, i, j);
+      xs_add(&acc, (AT(m, s->ig, i, j) + AT(m, s->ig, i, j + 1)) * AT(m, s->iv, i, j));
+    double sp = xs_value(&acc);
     sp = sp * 2.0 / N / RADIUS / m->dlat;
     for (int i = 1; i <= N; ++i) AT(m, mt, i, j) = sp;
   }
   {
     int j = M;
-    double np = 0.0;
+    xsum acc;
+    xs_init(&acc);
     for (int i = 1; i <= N; ++i)
-      np = np - (AT(m, s->ig, i, j) + AT(m, s->ig, i, j - 1)) * AT(m, s->iv, i, j - 1);
+      xs_add(&acc, (AT(m, s->ig, i, j) + AT(m, s->ig, i, j - 1)) * AT(m, s->iv, i, j - 1));
+    double np = -xs_value(&acc);
     np = np * 2.0 / N / RADIUS / m->dlat;
     for (int i = 1; i <= N; ++i) AT(m, mt, i, j) = np;
   }
@@ -498,19 +590,24 @@ static void mass_divergence(gdo_model* m, const state_t* s, tend_t* t) {
 static void filter_tend_row(gdo_model* m, const double* fac, double* trow,
                             const double* w1, const double* w2) {
   int N = m->N;
-  double s1 = 0.0, s2 = 0.0, a1 = 0.0, a2 = 0.0;
+  double s1, s2, a1 = 0.0, a2 = 0.0;
+  xsum acc;
+  xs_init(&acc);
   for (int i = 1; i <= N; ++i) {
     double t = trow[i + 1] * (w2 ? (w1[i + 1] + w2[i + 1]) : w1[i + 1]);
-    s1 = s1 + t;
+    xs_add(&acc, t);
     a1 = a1 + fabs(t);
   }
+  s1 = xs_value(&acc);
   if (fabs(s1) > 1.0e-16) { /* src/filter_mod.F90:31 */
     filter_row(m, fac, trow);
+    xs_init(&acc);
     for (int i = 1; i <= N; ++i) {
       double t = trow[i + 1] * (w2 ? (w1[i + 1] + w2[i + 1]) : w1[i + 1]);
-      s2 = s2 + t;
+      xs_add(&acc, t);
       a2 = a2 + fabs(t);
     }
+    s2 = xs_value(&acc);
     if (m->rescale_rtol > 0 && (fabs(s1) <= m->rescale_rtol * a1 || fabs(s2) <= m->rescale_rtol * a2)) return;
     for (int i = 1; i <= N; ++i) trow[i + 1] = trow[i + 1] * s1 / s2;
   }
@@ -598,33 +695,35 @@ static void update_state(gdo_model* m, double dt, const tend_t* t, const state_t
 /* src/types_mod.F90:347-371 */
 static double ip_tend_tend(const gdo_model* m, const tend_t* a, const tend_t* b) {
   int N = m->N, M = m->M, Mh = m->Mh;
-  double res = 0.0;
+  xsum res;
+  xs_init(&res);
   for (int j = 2; j <= M - 1; ++j)
     for (int i = 1; i <= N; ++i)
-      res = res + AT(m, a->a[T_DU], i, j) * AT(m, b->a[T_DU], i, j) * m->full_cos[j];
+      xs_add(&res, AT(m, a->a[T_DU], i, j) * AT(m, b->a[T_DU], i, j) * m->full_cos[j]);
   for (int j = 1; j <= Mh; ++j)
     for (int i = 1; i <= N; ++i)
-      res = res + AT(m, a->a[T_DV], i, j) * AT(m, b->a[T_DV], i, j) * m->half_cos[j];
+      xs_add(&res, AT(m, a->a[T_DV], i, j) * AT(m, b->a[T_DV], i, j) * m->half_cos[j]);
   for (int j = 1; j <= M; ++j)
     for (int i = 1; i <= N; ++i)
-      res = res + AT(m, a->a[T_DGD], i, j) * AT(m, b->a[T_DGD], i, j) * m->full_cos[j];
-  return res;
+      xs_add(&res, AT(m, a->a[T_DGD], i, j) * AT(m, b->a[T_DGD], i, j) * m->full_cos[j]);
+  return xs_value(&res);
 }
 
 /* src/types_mod.F90:373-397 */
 static double ip_tend_state(const gdo_model* m, const tend_t* a, const state_t* s) {
   int N = m->N, M = m->M, Mh = m->Mh;
-  double res = 0.0;
+  xsum res;
+  xs_init(&res);
   for (int j = 2; j <= M - 1; ++j)
     for (int i = 1; i <= N; ++i)
-      res = res + AT(m, a->a[T_DU], i, j) * AT(m, s->iu, i, j) * m->full_cos[j];
+      xs_add(&res, AT(m, a->a[T_DU], i, j) * AT(m, s->iu, i, j) * m->full_cos[j]);
   for (int j = 1; j <= Mh; ++j)
     for (int i = 1; i <= N; ++i)
-      res = res + AT(m, a->a[T_DV], i, j) * AT(m, s->iv, i, j) * m->half_cos[j];
+      xs_add(&res, AT(m, a->a[T_DV], i, j) * AT(m, s->iv, i, j) * m->half_cos[j]);
   for (int j = 1; j <= M; ++j)
     for (int i = 1; i <= N; ++i)
-      res = res + AT(m, a->a[T_DGD], i, j) * AT(m, s->gd, i, j) * m->full_cos[j];
-  return res;
+      xs_add(&res, AT(m, a->a[T_DGD], i, j) * AT(m, s->gd, i, j) * m->full_cos[j]);
+  return xs_value(&res);
 }
 
 /* src/dycore_mod.F90:754-792 */
@@ -774,15 +873,25 @@ static void ordinary_diffusion(gdo_model* m, double dt, state_t* s) {
                                (m->full_dlat[j] * m->full_dlat[j]) * fc[j];
     {
       int j = 1;
-      double sp = 0.0;
-      for (int i = 1; i <= N; ++i) sp = sp + AT(m, gd, i, j + 1) - AT(m, gd, i, j);
+      xsum acc;
+      xs_init(&acc);
+      for (int i = 1; i <= N; ++i) {
+        xs_add(&acc, AT(m, gd, i, j + 1));
+        xs_add(&acc, -AT(m, gd, i, j));
+      }
+      double sp = xs_value(&acc);
       double val = sp * hc[j] / (m->full_dlat[j] * m->full_dlat[j]) * fc[j] / N;
       for (int i = -1; i <= N + 2; ++i) AT(m, gdd, i, j) = val;
     }
     {
       int j = M;
-      double np = 0.0;
-      for (int i = 1; i <= N; ++i) np = np - (AT(m, gd, i, j) - AT(m, gd, i, j - 1));
+      xsum acc;
+      xs_init(&acc);
+      for (int i = 1; i <= N; ++i) {
+        xs_add(&acc, -AT(m, gd, i, j));
+        xs_add(&acc, AT(m, gd, i, j - 1));
+      }
+      double np = xs_value(&acc);
       double val = np * hc[j - 1] / (m->full_dlat[j] * m->full_dlat[j]) * fc[j] / N;
       for (int i = -1; i <= N + 2; ++i) AT(m, gdd, i, j) = val;
     }
@@ -851,23 +960,25 @@ static void ordinary_diffusion(gdo_model* m, double dt, state_t* s) {
 /* src/diag_mod.F90:71-87, 98-121 */
 static int diag_run(gdo_model* m, const state_t* s) {
   int N = m->N, M = m->M, Mh = m->Mh;
-  double mass = 0.0;
+  xsum am, ae;
+  xs_init(&am);
+  xs_init(&ae);
   for (int j = 1; j <= M; ++j)
     for (int i = 1; i <= N; ++i)
-      mass = mass + m->full_cos[j] * m->dlon * m->dlat * AT(m, s->gd, i, j);
-  mass = mass * (RADIUS * RADIUS);
-  double e = 0.0;
+      xs_add(&am, m->full_cos[j] * m->dlon * m->dlat * AT(m, s->gd, i, j));
+  double mass = xs_value(&am) * (RADIUS * RADIUS);
   for (int j = 2; j <= M - 1; ++j)
     for (int i = 1; i <= N; ++i)
-      e = e + AT(m, s->iu, i, j) * AT(m, s->iu, i, j) * m->full_cos[j];
+      xs_add(&ae, AT(m, s->iu, i, j) * AT(m, s->iu, i, j) * m->full_cos[j]);
   for (int j = 1; j <= Mh; ++j)
     for (int i = 1; i <= N; ++i)
-      e = e + AT(m, s->iv, i, j) * AT(m, s->iv, i, j) * m->half_cos[j];
+      xs_add(&ae, AT(m, s->iv, i, j) * AT(m, s->iv, i, j) * m->half_cos[j]);
   for (int j = 1; j <= M; ++j)
     for (int i = 1; i <= N; ++i) {
       double h = AT(m, s->gd, i, j) + AT(m, m->ghs, i, j);
-      e = e + h * h * m->full_cos[j];
+      xs_add(&ae, h * h * m->full_cos[j]);
     }
+  double e = xs_value(&ae);
   m->total_mass = mass;
   m->total_energy = e;
   return (isnan(mass) || isnan(e)) ? 1 : 0;

@@ -39,6 +39,8 @@ void gdo_destroy(gdo_model* m);
 /* Extension guard of the filter rescale (0 = reference behaviour); the
  * CUDA path's gdc_params::filter_rescale_rtol. */
 void gdo_set_rescale_rtol(gdo_model* m, double rtol);
+/* The oracle's correctly rounded sum (exposed for its self-test). */
+double gdo_fsum(const double* x, int n);
 
 /* Initial-condition hook: copies u, v, gd, ghs (padded layout) into
  * state(1) and static, as the reference's test-case modules do. */

@@ -13,15 +13,16 @@ import numpy as np
 
 from . import build as _build
 
-_lib = None
+_libs = {}
 _P = ctypes.POINTER(ctypes.c_double)
 
 
-def lib() -> ctypes.CDLL:
-    global _lib
-    if _lib is None:
-        path = _build.build()
-        L = ctypes.CDLL(str(path))
+def lib(fast: bool = False) -> ctypes.CDLL:
+    """The checker (exact sums), or with fast=True the timing build of the
+    CPU baseline (plain sums, -Ofast like the reference)."""
+    if fast not in _libs:
+        _build.build()
+        L = ctypes.CDLL(str(_build.LIB_FAST if fast else _build.LIB))
         vp, dp, i = ctypes.c_void_p, _P, ctypes.c_int
         ip = ctypes.POINTER(ctypes.c_int)
         L.gdo_create.restype = vp
@@ -29,6 +30,8 @@ def lib() -> ctypes.CDLL:
                                  ctypes.c_double, i]
         L.gdo_destroy.argtypes = [vp]
         L.gdo_set_rescale_rtol.argtypes = [vp, ctypes.c_double]
+        L.gdo_fsum.argtypes = [dp, i]
+        L.gdo_fsum.restype = ctypes.c_double
         L.gdo_set_state.argtypes = [vp, dp, dp, dp, dp]
         L.gdo_run_init.argtypes = [vp]
         L.gdo_step.argtypes = [vp, i]
@@ -50,6 +53,12 @@ def _ptr(a):
     return a.ctypes.data_as(_P)
 
 
+def fsum(x) -> float:
+    """The oracle's correctly rounded summation."""
+    a = np.ascontiguousarray(x, dtype=np.float64)
+    return lib().gdo_fsum(_ptr(a), len(a))
+
+
 def _pad(rows, N):
     return np.zeros((rows + 4, N + 4))
 
@@ -59,16 +68,18 @@ class OracleModel:
 
     def __init__(self, num_lon, num_lat, time_step_size, subcycles=4, split_scheme=0, qcon_modified=1,
                  uv_adv_scheme=0, upwind_lon_beta=0.0, upwind_lat_beta=0.5, use_zonal_tend_filter=1,
-                 cutoff=(), use_diffusion=0, diffusion_coef=0.0, diffusion_order=2, rescale_rtol=0.0):
+                 cutoff=(), use_diffusion=0, diffusion_coef=0.0, diffusion_order=2, rescale_rtol=0.0,
+                 fast=False):
         self.N, self.M = num_lon, num_lat
+        self._L = lib(fast)
         c = (ctypes.c_int * 20)(*([0] * 20))
         for k, x in enumerate(cutoff):
             c[k] = int(x)
-        self.h = lib().gdo_create(num_lon, num_lat, time_step_size, subcycles, split_scheme, qcon_modified,
+        self.h = self._L.gdo_create(num_lon, num_lat, time_step_size, subcycles, split_scheme, qcon_modified,
                                   uv_adv_scheme, upwind_lon_beta, upwind_lat_beta, use_zonal_tend_filter, c,
                                   use_diffusion, diffusion_coef, diffusion_order)
         if rescale_rtol:
-            lib().gdo_set_rescale_rtol(self.h, rescale_rtol)
+            self._L.gdo_set_rescale_rtol(self.h, rescale_rtol)
 
     @classmethod
     def from_params(cls, p):
@@ -80,50 +91,50 @@ class OracleModel:
 
     def set_state(self, u, v, gd, ghs):
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (u, v, gd, ghs)]
-        lib().gdo_set_state(self.h, *map(_ptr, arrs))
-        lib().gdo_run_init(self.h)
+        self._L.gdo_set_state(self.h, *map(_ptr, arrs))
+        self._L.gdo_run_init(self.h)
 
     def step(self, n=1):
-        return lib().gdo_step(self.h, n)
+        return self._L.gdo_step(self.h, n)
 
     def get_state(self):
         N, M = self.N, self.M
         u, v, gd = _pad(M, N), _pad(M - 1, N), _pad(M, N)
         iu, iv, ig = _pad(M, N), _pad(M - 1, N), _pad(M, N)
-        lib().gdo_get_state(self.h, _ptr(u), _ptr(v), _ptr(gd), _ptr(iu), _ptr(iv), _ptr(ig))
+        self._L.gdo_get_state(self.h, _ptr(u), _ptr(v), _ptr(gd), _ptr(iu), _ptr(iv), _ptr(ig))
         return dict(u=u, v=v, gd=gd, iu=iu, iv=iv, ig=ig)
 
     def diag(self):
         m, e, b = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
-        lib().gdo_diag(self.h, ctypes.byref(m), ctypes.byref(e), ctypes.byref(b))
+        self._L.gdo_diag(self.h, ctypes.byref(m), ctypes.byref(e), ctypes.byref(b))
         return m.value, e.value, b.value
 
     def tendency(self, pass_=0):
         N, M = self.N, self.M
         du, dv, dgd = _pad(M, N), _pad(M - 1, N), _pad(M, N)
-        lib().gdo_tendency(self.h, pass_, _ptr(du), _ptr(dv), _ptr(dgd))
+        self._L.gdo_tendency(self.h, pass_, _ptr(du), _ptr(dv), _ptr(dgd))
         return du, dv, dgd
 
     def antisymmetry(self):
         out = np.zeros(4)
-        lib().gdo_antisymmetry(self.h, _ptr(out))
+        self._L.gdo_antisymmetry(self.h, _ptr(out))
         return out
 
     def filter_row(self, half, lat_idx, x):
         x = np.ascontiguousarray(x, dtype=np.float64).copy()
-        lib().gdo_filter_row(self.h, int(half), int(lat_idx), _ptr(x))
+        self._L.gdo_filter_row(self.h, int(half), int(lat_idx), _ptr(x))
         return x
 
     def filter_flags(self):
         M = self.M
         ff, fh = (ctypes.c_int * M)(), (ctypes.c_int * (M - 1))()
         cf, ch = (ctypes.c_int * M)(), (ctypes.c_int * (M - 1))()
-        lib().gdo_filter_flags(self.h, ff, fh, cf, ch)
+        self._L.gdo_filter_flags(self.h, ff, fh, cf, ch)
         return list(ff), list(fh), list(cf), list(ch)
 
     def close(self):
         if self.h:
-            lib().gdo_destroy(self.h)
+            self._L.gdo_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -1,16 +1,12 @@
 """CUDA path vs the CPU oracle, through the C ABI (FP64 plain path).
 
-The FP64 kernels are compiled without FMA contraction, so every point-wise
-expression rounds exactly as the oracle's; the two differ only in the order
-of their sums (filter s1/s2 and projections, pole caps, beta, diagnostics).
-
-Tolerances (FP64): operator level (one space_operators call) relative L2
-<= 1e-13 for du and dv, <= 1e-11 for dgd (on filtered rows s1 = sum of
-dgd*(gd+ghs) inherits the near-cancellation of the row's mass flux, so the
-rescale factor s1/s2 carries ~1e-12 of summation-order noise); one model
-step <= 1e-12; config 0 (360x181, dt 240 s, csp2 with 6 subcycles, filter
-4,4,4,4,4) after 360 steps: relative L2 of gd, u, v <= 1e-12, and the
-total-mass drift equal to the oracle's within 1e-13.
+The FP64 kernels and the host tables are compiled without FMA contraction,
+so every point-wise expression rounds exactly as the oracle's, and every
+sum (filter s1/s2 and projections, pole caps, beta, diagnostics) is the
+correctly rounded sum on both sides.  The plain path is therefore expected
+to be bitwise identical to the oracle; the stated bound (relative L2
+<= 1e-12 after 360 steps of config 0, mass drift equal within 1e-13) is
+asserted as well.
 """
 import numpy as np
 import pytest
@@ -42,34 +38,28 @@ def test_tendency_parity(native, pass_, adv):
     for name, a, b in zip(("du", "dv", "dgd"), g, r):
         if pass_ == 2 and name == "dgd":
             assert np.all(interior(a) == 0)
-            continue
-        tol = 1e-11 if name == "dgd" else 1e-13
-        assert rel_l2(a, b) <= tol, (name, rel_l2(a, b))
-        assert rel_linf(a, b) <= 100 * tol, (name, rel_linf(a, b))
+        assert np.array_equal(interior(a), interior(b)), (name, rel_l2(a, b))
 
 
-@pytest.mark.parametrize("split", [gdc.SPLIT_NONE, gdc.SPLIT_CSP2, gdc.SPLIT_ISP])
-def test_step_parity(native, split):
+@pytest.mark.parametrize("split,adv", [(gdc.SPLIT_NONE, 0), (gdc.SPLIT_CSP2, 0), (gdc.SPLIT_ISP, 0),
+                                       (gdc.SPLIT_CSP2, 1)])
+def test_step_parity(native, split, adv):
     N, M = 180, 91
-    p = scheme(gdc, N, M, 480.0, split=split, cutoff=(3, 3, 3))
+    # Without splitting the gravity-wave step must satisfy the CFL limit of
+    # the first unfiltered row (~110 s at 2 degrees): dt 90 s.
+    dt = 90.0 if split == gdc.SPLIT_NONE else 480.0
+    p = scheme(gdc, N, M, dt, split=split, cutoff=(3, 3, 3), adv=adv, lat_beta=0.5, lon_beta=0.25)
     ic = gdc.ic_seeded(N, M, seed=2)
     m, o = pair(p, ic)
-    m.run(1)
-    o.step(1)
-    s = o.get_state()
-    u, v, gd = m.get_state()
-    for a, b in ((gd, s["gd"]), (u, s["u"]), (v, s["v"])):
-        assert rel_l2(a, b) <= 1e-12
-    m.run(9)
-    o.step(9)
-    s = o.get_state()
-    u, v, gd = m.get_state()
-    for a, b in ((gd, s["gd"]), (u, s["u"]), (v, s["v"])):
-        assert rel_l2(a, b) <= 1e-12
-    mg, eg, bg = m.diag()
-    mo, eo, bo = o.diag()
-    assert abs(mg - mo) / mo < 1e-13 and abs(eg - eo) / eo < 1e-12
-    assert abs(bg - bo) < 1e-9
+    for n in (1, 9):
+        m.run(n)
+        o.step(n)
+        s = o.get_state()
+        u, v, gd = m.get_state()
+        for a, b in ((gd, s["gd"]), (u, s["u"]), (v, s["v"])):
+            assert rel_l2(a, b) <= 1e-12
+            assert np.array_equal(interior(a), interior(b))
+    assert m.diag() == o.diag()
 
 
 def test_diffusion_parity(native):
@@ -86,6 +76,7 @@ def test_diffusion_parity(native):
     u, v, gd = m.get_state()
     for a, b in ((gd, s["gd"]), (u, s["u"]), (v, s["v"])):
         assert rel_l2(a, b) <= 1e-12
+        assert np.array_equal(interior(a), interior(b))
 
 
 @pytest.mark.slow
@@ -103,6 +94,8 @@ def test_config0_360_steps(native):
     u, v, gd = m.get_state()
     errs = {k: rel_l2(a, s[k]) for k, a in (("gd", gd), ("u", u), ("v", v))}
     assert all(e <= 1e-12 for e in errs.values()), errs
+    for k, a in (("gd", gd), ("u", u), ("v", v)):
+        assert np.array_equal(interior(a), interior(s[k])), k
     m1, _, _ = m.diag()
     o1, _, _ = o.diag()
     drift_g, drift_o = (m1 - m0) / m0, (o1 - o0) / o0

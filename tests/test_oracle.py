@@ -14,6 +14,21 @@ from helpers import interior
 from oracle.oracle import OracleModel
 
 
+def test_correctly_rounded_sum():
+    """The oracle's sums are correctly rounded (compared with math.fsum)."""
+    import math
+    from oracle.oracle import fsum
+    rng = np.random.default_rng(0)
+    for trial in range(200):
+        n = int(rng.integers(1, 3000))
+        x = rng.standard_normal(n) * np.exp(rng.uniform(-40, 40, n))
+        if trial % 3 == 0:  # heavy cancellation
+            x = np.concatenate([x, -x[: n // 2] * (1 + 1e-15)])
+        assert fsum(x) == math.fsum(x)
+    assert fsum([1e16, 1.0, -1e16]) == 1.0
+    assert fsum([]) == 0.0
+
+
 def fftpack_projection(x, c):
     """FFTPACK rfft1f -> keep packed indices 1..2(c+1) -> rfft1b, via numpy."""
     N = len(x)
