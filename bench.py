@@ -145,14 +145,22 @@ def dist_setup(n_gpus):
     return rank, world, dist
 
 
-def reduce_max(dist, x: float) -> float:
+def reduce_max(dist, x: float, device: str = "cuda") -> float:
     """Max over ranks (replicas): the job is done when the slowest replica is."""
     if dist is None:
         return x
     import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_value(dist, points_per_rank: float, ms: float, device: str = "cuda") -> tuple[float, float]:
+    """Whole-job throughput of N independent replicas: all ranks' grid points
+    over the slowest rank's time.  Returns (value, max ms)."""
+    world = dist.get_world_size() if dist is not None else 1
+    ms_all = reduce_max(dist, ms, device)
+    return world * points_per_rank / (ms_all / 1e3), ms_all
 
 
 def barrier(dist):
@@ -297,8 +305,7 @@ def run_ours(args, rank, world, dist):
         ms, gpt, launches, active_steps, nan = time_batch(gdc, torch, members, args.steps, args.warmup,
                                                           gdc.FP32, ts)
     clocks = clk.summary()
-    ms_all = reduce_max(dist, ms)
-    value = world * gpt / (ms_all / 1e3)
+    value, ms_all = replica_value(dist, gpt, ms)
     plain = plain_fp64(gdc, torch, ts)
     e2e_ms, e2e_gpt, h2d, d2h = e2e_batch(gdc, torch, members, args.steps, gdc.FP32)
     e2e_ms = reduce_max(dist, e2e_ms)
