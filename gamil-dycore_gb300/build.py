@@ -58,7 +58,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     OUT.mkdir(exist_ok=True)
     lib = OUT / "libgdc.so"
     headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [INCLUDE / "gdc.h"]
-    cu = [CSRC / "gdc_kernels_f64.cu", CSRC / "gdc_kernels_f32.cu"]
+    cu = [CSRC / "gdc_kernels_f64.cu", CSRC / "gdc_kernels_f32.cu", CSRC / "gdc_noalloc.cu"]
     cpp = [CSRC / "gdc_engine.cpp", CSRC / "gdc_host.cpp"]
     if force or _stale(lib, cu + cpp + headers):
         cmds, objs = [], []
@@ -66,7 +66,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
             obj = OUT / (src.stem + ".o")
             objs.append(obj)
             # The FP64 unit keeps the reference's rounding: no FMA contraction.
-            fmad = ["--fmad=false"] if src.stem.endswith("_f64") else []
+            fmad = ["--fmad=false"] if src.stem.endswith(("_f64", "_noalloc")) else []
             cmds.append([nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", *fmad, "-Xcompiler",
                          "-fPIC,-ffp-contract=off", f"-I{INCLUDE}", "-c", str(src), "-o", str(obj)])
         for src in cpp:

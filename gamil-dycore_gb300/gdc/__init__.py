@@ -127,6 +127,9 @@ def lib() -> ctypes.CDLL:
             "gdc_batch_autotune": (ctypes.c_int, [vp, ip, ip, dp]),
             "gdc_batch_profile": (ctypes.c_int, [vp, ctypes.c_int, dp, i64p]),
             "gdc_algorithmic_bytes_per_gpt_step": (ctypes.c_double, [ctypes.POINTER(Params)]),
+            "gdc_tendency_noalloc": (ctypes.c_int, [ctypes.POINTER(Params), ctypes.c_int, vp, vp, vp, vp, vp, vp,
+                                                    vp, vp, vp, vp]),
+            "gdc_noalloc_last_error": (ctypes.c_char_p, []),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -306,6 +309,19 @@ class Model:
             self.close()
         except Exception:
             pass
+
+
+def tendency_noalloc(params: Params, pass_: int, gd: int, iap_u: int, iap_v: int, ghs: int, du: int, dv: int,
+                     dgd: int, given_u: int | None = None, given_v: int | None = None, stream: int | None = None):
+    """space_operators into caller-owned device buffers (interior layout,
+    FP64), without any device allocation by the library.  Arguments are
+    device addresses (e.g. torch tensors' data_ptr())."""
+    vp = ctypes.c_void_p
+    rc = lib().gdc_tendency_noalloc(ctypes.byref(params), pass_, vp(gd), vp(iap_u), vp(iap_v), vp(ghs),
+                                    vp(given_u) if given_u else None, vp(given_v) if given_v else None,
+                                    vp(du), vp(dv), vp(dgd), vp(stream) if stream else None)
+    if rc:
+        raise GdcError(rc, lib().gdc_noalloc_last_error().decode())
 
 
 class Batch:

@@ -144,6 +144,30 @@ int gdc_debug_tendency(gdc_handle* h, int pass, double* du, double* dv,
  * NULL restores the handle's own stream). */
 int gdc_set_stream(gdc_handle* h, void* cuda_stream);
 
+/* No counterpart in the reference: space_operators (as gdc_debug_tendency)
+ * for callers that cannot allocate device memory -- code inside CUDA-graph
+ * stream capture, hosts whose allocator owns all device memory, plug-ins
+ * that must not grow the device footprint.  FP64 only.  All pointers are
+ * the CALLER's device buffers in the interior layout (rows x num_lon,
+ * longitude fastest, no halo): gd, iap_u, ghs, du, dgd num_lat rows;
+ * iap_v, dv num_lat-1 rows; given_u/given_v (both or neither) are u, v to
+ * use as given (e.g. an initial condition's own u, v), NULL to derive them
+ * from the iap fields.  The library keeps its descriptor, work list and
+ * tables in one 2 MiB static device array (held by every GPU that loads the
+ * library until exit), so grids are limited to 1440 x 721; larger grids
+ * return GDC_E_CONFIG.  It calls no cudaMalloc / cudaFree.  The first call
+ * on a device resolves the array's device address -- make it before any
+ * stream capture.  All calls share the array: calls that overlap on the
+ * GPU race (serialise them on one stream).  Enqueued on `cuda_stream`;
+ * returns before the kernel finishes.  The message of a failure is
+ * gdc_noalloc_last_error(). */
+int gdc_tendency_noalloc(const gdc_params* p, int pass, const double* gd,
+                         const double* iap_u, const double* iap_v,
+                         const double* ghs, const double* given_u,
+                         const double* given_v, double* du, double* dv,
+                         double* dgd, void* cuda_stream);
+const char* gdc_noalloc_last_error(void);
+
 /* ---- initial conditions (host only, no GPU) ------------------------- */
 /* src/test_cases/barotropic/rossby_haurwitz_wave_test_mod.F90:33-85
  * (R = 4, omg = 7.848e-6, gd0 = 8000 g). */
