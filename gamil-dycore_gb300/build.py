@@ -66,7 +66,9 @@ def build(force: bool = False, verbose: bool = False) -> Path:
             obj = OUT / (src.stem + ".o")
             objs.append(obj)
             # The FP64 unit keeps the reference's rounding: no FMA contraction.
-            fmad = ["--fmad=false"] if src.stem.endswith(("_f64", "_noalloc")) else []
+            # The FP32 unit uses fast single-precision division and square
+            # root (fast math affects single precision only).
+            fmad = ["--fmad=false"] if src.stem.endswith(("_f64", "_noalloc")) else ["--use_fast_math"]
             cmds.append([nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", *fmad, "-Xcompiler",
                          "-fPIC,-ffp-contract=off", f"-I{INCLUDE}", "-c", str(src), "-o", str(obj)])
         for src in cpp:

@@ -156,6 +156,8 @@ class Batch final : public BatchIface {
           int* id) override {
     if (N < 8 || M < 5 || ld < N + 4 || !(dt > 0) || nsteps < 0 || !u || !v || !gd || !ghs)
       return fail(GDC_E_CONFIG, "add: invalid grid, time step, length or buffers");
+    if (N % 4 != 0)
+      return fail(GDC_E_CONFIG, "add: num_lon must be a multiple of 4 (tile rows are copied 16 bytes at a time)");
     gdc_params mp = P;  // this member's filter rows
     if (cutoff)
       for (int k = 0; k < 20; ++k) mp.zonal_tend_filter_cutoff_wavenumber[k] = cutoff[k];
@@ -511,8 +513,8 @@ class Batch final : public BatchIface {
       r = 8;
       c = default_cols();
     }
-    if (r < 1 || r > 32 || c < 8 || c > 256 || r * c > 512)
-      return fail(GDC_E_CONFIG, "set_tile: rows in 1..32, cols in 8..256, rows*cols <= 512");
+    if (!tile_shape_supported(r, c))
+      return fail(GDC_E_CONFIG, "set_tile: supported shapes are 8x32, 8x64 and 4x128");
     tile_r = r;
     tile_c = c;
     dirty = true;
@@ -529,7 +531,7 @@ class Batch final : public BatchIface {
   // Times each candidate tile shape on the current members (graph replay,
   // CUDA events) and keeps the fastest.  Advances the members.
   int autotune(int* rr, int* cc, double* best_ms) override {
-    static const int cand[][2] = {{4, 32}, {8, 32}, {16, 32}, {4, 64}, {8, 64}, {2, 128}, {4, 128}, {16, 16}, {2, 256}};
+    static const int cand[][2] = {{8, 32}, {8, 64}, {4, 128}};
     double best = 1e30;
     int br = tile_r, bc = tile_c;
     for (auto& c : cand) {
@@ -1253,8 +1255,8 @@ int gdc_create(const gdc_params* p, gdc_handle** out) {
     std::fprintf(stderr, "gdc_create: %s\n", err.c_str());
     return rc;
   }
-  if (p->num_lon < 8 || p->num_lat < 5 || !(p->time_step_size > 0)) {
-    std::fprintf(stderr, "gdc_create: invalid num_lon, num_lat or time_step_size\n");
+  if (p->num_lon < 8 || p->num_lat < 5 || p->num_lon % 4 != 0 || !(p->time_step_size > 0)) {
+    std::fprintf(stderr, "gdc_create: invalid num_lon (>= 8, multiple of 4), num_lat or time_step_size\n");
     return GDC_E_CONFIG;
   }
   auto* h = new gdc_handle();

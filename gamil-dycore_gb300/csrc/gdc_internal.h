@@ -166,7 +166,12 @@ struct DiagArgs {
   long long* nan_step;   // per member: first step with NaN mass/energy
 };
 
-// Kernel launchers (gdc_kernels.cu).  `smem_limit` is the opt-in maximum.
+// Tile shapes compiled for the stage and diffusion kernels (rows x columns).
+inline bool tile_shape_supported(int r, int c) {
+  return (r == 8 && c == 32) || (r == 8 && c == 64) || (r == 4 && c == 128);
+}
+
+// Kernel launchers (gdc_kernels_f64.cu / gdc_kernels_f32.cu).
 template <typename T>
 int launch_stage(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int adv, int tile_rows,
                  int tile_cols, int max_n, const StageArgs& a, void* stream);

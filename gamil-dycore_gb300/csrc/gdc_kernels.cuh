@@ -39,7 +39,6 @@ namespace gdc {
 constexpr int kThreads = 256;
 constexpr int kRowChunk = 128;  // columns per chunk of a whole-row task
 constexpr int kMaxKeep = 128;   // packed FFT coefficients a filter row may keep
-constexpr int kPPT = 2;         // tile points per thread (tile <= 512 points)
 
 // ------------------------------------------------------------ helpers
 
@@ -77,19 +76,37 @@ __device__ inline A warp_sum(A v) {
   return v;
 }
 
+// Plain FP64 running sum (the FP32 path's diagnostics: FP64, but without
+// the double-double cost -- FP64 arithmetic is the scarce unit).
+struct PlainD {
+  double s = 0, c = 0;
+  __device__ void add(double x) { s += x; }
+  __device__ void merge(double os, double oc) { s += os + oc; }
+  __device__ double value() const { return s + c; }
+};
 template <typename T>
-__device__ inline void warp_acc(Acc<T>& a) {
+struct DiagAcc {
+  using type = Acc<double>;
+};
+template <>
+struct DiagAcc<float> {
+  using type = PlainD;
+};
+
+template <typename A>
+__device__ inline void warp_acc(A& a) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    const T os = __shfl_xor_sync(0xffffffffu, a.s, o);
-    const T oc = __shfl_xor_sync(0xffffffffu, a.c, o);
+    const auto os = __shfl_xor_sync(0xffffffffu, a.s, o);
+    const auto oc = __shfl_xor_sync(0xffffffffu, a.c, o);
     a.merge(os, oc);
   }
 }
 
-// Block-wide accumulation; `red` holds 64 T.  Every thread gets the result.
-template <typename T>
-__device__ Acc<T> block_acc(Acc<T> a, T* red) {
+// Block-wide accumulation; `red` holds 64 values.  Every thread gets the
+// result.
+template <typename A, typename V>
+__device__ A block_acc(A a, V* red) {
   warp_acc(a);
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
   __syncthreads();
@@ -99,7 +116,7 @@ __device__ Acc<T> block_acc(Acc<T> a, T* red) {
   }
   __syncthreads();
   if (w == 0) {
-    Acc<T> b;
+    A b;
     if (l < nw) {
       b.s = red[2 * l];
       b.c = red[2 * l + 1];
@@ -111,15 +128,15 @@ __device__ Acc<T> block_acc(Acc<T> a, T* red) {
     }
   }
   __syncthreads();
-  Acc<T> r;
+  A r;
   r.s = red[0];
   r.c = red[1];
   __syncthreads();
   return r;
 }
 
-template <typename T>
-__device__ inline T block_value(Acc<T> a, T* red) {
+template <typename A, typename V>
+__device__ inline V block_value(A a, V* red) {
   return block_acc(a, red).value();
 }
 
@@ -135,13 +152,6 @@ __device__ __forceinline__ void cp_async(T* smem, const T* gmem, bool valid) {
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 template <typename T>
-struct TileSmem {
-  T *gd, *ghs, *iu, *iv, *ig, *u, *v;
-  int R, W, SW, rows;  // SW = W + 3 columns, rows = R + 3
-  int j0, i0;
-};
-
-template <typename T>
 __device__ inline T cf(const MemberDev<T>& md, int k, int j) {
   return md.coef[cf_off(k, md.M) + j];
 }
@@ -150,17 +160,45 @@ __device__ inline T ch(const MemberDev<T>& md, int k, int jh) {  // jh in -1..Mh
   return md.coef[ch_off(k, md.M) + jh + 1];
 }
 
-// Partition of a staging buffer into the seven tile arrays.
-template <typename T>
-__device__ TileSmem<T> carve_tile(T* base, int R, int W, int j0, int i0) {
-  TileSmem<T> t;
-  t.R = R;
-  t.W = W;
-  t.SW = W + 3;
-  t.rows = R + 3;
-  t.j0 = j0;
-  t.i0 = i0;
-  const int n = t.rows * t.SW;
+// Shared-memory tile of R x W output points with compile-time shape: rows
+// j0-1 .. j0+R+1 and columns i0-1 .. i0+W+1 of gd, ghs, iap u, iap v, plus
+// the derived iap gd, u and v.  Rows are padded so that column i0 starts on
+// a 16-byte boundary (the row interiors are copied 16 bytes at a time).
+// Partial tiles (the last row band of a run, the last column block of a
+// row) stage only what their valid points use.  `cfull` / `chalf` hold the
+// row coefficients of full rows j0-1..j0+R and half rows j0-1..j0+R.
+template <typename T, int R_, int W_>
+struct Tile {
+  static constexpr int R = R_, W = W_;
+  static constexpr int VEC = 16 / (int)sizeof(T);  // elements per 16-byte copy
+  static constexpr int OFF = VEC - 1;              // so that column i0 is aligned
+  static constexpr int SW = ((W_ + 3 + OFF + VEC - 1) / VEC) * VEC;
+  static constexpr int ROWS = R_ + 3, NS = ROWS * SW;
+  static constexpr int CR = R_ + 2;                // coefficient rows
+  T *gd, *ghs, *iu, *iv, *ig, *u, *v;
+  T *cfull, *chalf;
+  int j0, i0, vrows, vcols;
+  __device__ static int pos(int rr, int cc) { return rr * SW + cc + OFF; }
+  __device__ T cf(int k, int j) const { return cfull[k * CR + (j - j0 + 1)]; }
+  __device__ T ch(int k, int jh) const { return chalf[k * CR + (jh - j0 + 1)]; }
+};
+
+// Full-row coefficients a tile reads, and the half-row ones.
+enum TileFull { TF_RADVLON, TF_RADVLAT, TF_F, TF_C, TF_C1, TF_C2, TF_DLON, TF_DLAT, TF_COS, TF_N };
+enum TileHalf { TH_COS, TH_RADVLON, TH_RADVLAT, TH_DLAT, TH_DLON, TH_N };
+__device__ __constant__ const int kTileFullSrc[TF_N] = {CF_RADVLON, CF_RADVLAT, CF_F, CF_C, CF_C1,
+                                                        CF_C2, CF_DLON, CF_DLAT, CF_COS};
+__device__ __constant__ const int kTileHalfSrc[TH_N] = {CH_COS, CH_RADVLON, CH_RADVLAT, CH_DLAT, CH_DLON};
+
+template <typename T, int R, int W>
+constexpr int tile_words() {
+  return 7 * Tile<T, R, W>::NS + (TF_N + TH_N) * Tile<T, R, W>::CR;
+}
+
+template <typename T, int R, int W>
+__device__ inline Tile<T, R, W> carve(T* base, int j0, int i0, int vrows, int vcols) {
+  Tile<T, R, W> t;
+  constexpr int n = Tile<T, R, W>::NS;
   t.gd = base;
   t.ghs = base + n;
   t.iu = base + 2 * n;
@@ -168,57 +206,114 @@ __device__ TileSmem<T> carve_tile(T* base, int R, int W, int j0, int i0) {
   t.ig = base + 4 * n;
   t.u = base + 5 * n;
   t.v = base + 6 * n;
+  t.cfull = base + 7 * n;
+  t.chalf = t.cfull + TF_N * Tile<T, R, W>::CR;
+  t.j0 = j0;
+  t.i0 = i0;
+  t.vrows = vrows;
+  t.vcols = vcols;
   return t;
 }
 
-// Issue the copies of rows j0-1 .. j0+R+1 (full and half), columns
-// i0-1 .. i0+W+1 (periodic) into the tile; completes at cp_async_wait_all.
-// With `given`, u and v are copied too (the level's u, v were supplied
-// with its state instead of being derived from it).
 template <typename T>
+__device__ __forceinline__ void cp_async16(T* smem, const T* gmem, bool valid) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  const int n = valid ? 16 : 0;
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(n) : "memory");
+}
+
+// Issue the tile's copies (completed by cp_async_wait_all).  Positions off
+// the sphere are zero-filled (the reference's never-filled latitude halo);
+// positions beyond a partial tile's halo are not staged and never read
+// (tile_derive masks them, the stencils stop at the halo).  With `given`, u and v
+// are copied too (the level's u, v were supplied with its state).  The
+// row interiors (columns i0 .. i0+vcols-1, never wrapping) go 16 bytes at a
+// time; the halo columns i0-1, i0+vcols, i0+vcols+1 element by element.
+// Requires num_lon and i0 to be multiples of VEC (checked at admission).
+template <typename T, int R, int W>
 __device__ void tile_issue(const MemberDev<T>& md, const T* __restrict__ gd, const T* __restrict__ iu,
-                           const T* __restrict__ iv, TileSmem<T>& t, bool given = false) {
+                           const T* __restrict__ iv, Tile<T, R, W>& t, bool given = false) {
+  using TL = Tile<T, R, W>;
+  constexpr int VEC = TL::VEC, NCH = W / VEC;
   const int N = md.N, M = md.M, Mh = md.Mh;
-  const int SW = t.SW, n = t.rows * SW;
-  for (int p = threadIdx.x; p < n; p += blockDim.x) {
-    const int rr = p / SW, cc = p - rr * SW;
+  const int nfield = given ? 6 : 4;
+  // interiors
+  for (int q = threadIdx.x; q < TL::ROWS * NCH; q += kThreads) {
+    const int rr = q / NCH, k = q - rr * NCH;
+    const int j = t.j0 - 1 + rr;
+    // Chunks past a partial tile are not issued at all: a zero-filling
+    // copy there would overlap the halo columns written by other threads.
+    if (rr > t.vrows + 2 || k * VEC >= t.vcols) continue;
+    const bool vf = j >= 0 && j < M, vh = j >= 0 && j < Mh;
+    const size_t o = vf ? (size_t)j * N + t.i0 + k * VEC : 0;
+    const int dp = TL::pos(rr, 1 + k * VEC);
+    cp_async16(&t.gd[dp], gd + o, vf);
+    cp_async16(&t.ghs[dp], md.ghs + o, vf);
+    cp_async16(&t.iu[dp], iu + o, vf);
+    cp_async16(&t.iv[dp], iv + (vh ? o : 0), vh);
+    if (given) {
+      cp_async16(&t.u[dp], md.given_u + o, vf);
+      cp_async16(&t.v[dp], md.given_v + (vh ? o : 0), vh);
+    }
+  }
+  // halo columns
+  for (int q = threadIdx.x; q < TL::ROWS * 3; q += kThreads) {
+    const int rr = q / 3, h = q - rr * 3;
+    const int cc = h == 0 ? 0 : t.vcols + h;
     const int j = t.j0 - 1 + rr;
     int i = t.i0 - 1 + cc;
     i = i < 0 ? i + N : (i >= N ? i - N : i);
-    const bool vf = (j >= 0 && j < M), vh = (j >= 0 && j < Mh);
+    if (rr > t.vrows + 2) continue;
+    const bool vf = j >= 0 && j < M, vh = j >= 0 && j < Mh;
     const size_t o = vf ? (size_t)j * N + i : 0;
-    cp_async(&t.gd[p], gd + o, vf);
-    cp_async(&t.ghs[p], md.ghs + o, vf);
-    cp_async(&t.iu[p], iu + o, vf);
-    cp_async(&t.iv[p], iv + (vh ? o : 0), vh);
+    const int dp = TL::pos(rr, cc);
+    cp_async(&t.gd[dp], gd + o, vf);
+    cp_async(&t.ghs[dp], md.ghs + o, vf);
+    cp_async(&t.iu[dp], iu + o, vf);
+    cp_async(&t.iv[dp], iv + (vh ? o : 0), vh);
     if (given) {
-      cp_async(&t.u[p], md.given_u + o, vf);
-      cp_async(&t.v[p], md.given_v + (vh ? o : 0), vh);
+      cp_async(&t.u[dp], md.given_u + o, vf);
+      cp_async(&t.v[dp], md.given_v + (vh ? o : 0), vh);
     }
+  }
+  (void)nfield;
+  // row coefficients of full rows j0-1..j0+R and half rows j0-1..j0+R
+  for (int q = threadIdx.x; q < (TF_N + TH_N) * TL::CR; q += kThreads) {
+    const int k = q / TL::CR, lr = q - k * TL::CR;
+    const int j = t.j0 - 1 + lr;
+    T val = T(0);
+    if (k < TF_N) {
+      if (j >= 0 && j < M) val = md.coef[cf_off(kTileFullSrc[k], M) + j];
+    } else if (j >= -1 && j <= Mh) {
+      val = md.coef[ch_off(kTileHalfSrc[k - TF_N], M) + j + 1];
+    }
+    t.cfull[q] = val;  // cfull and chalf are contiguous
   }
 }
 
-// After the copies: iap gd everywhere, then u on full rows j0..j0+R (local
-// 1..R+1; from local 0 when the stencil also needs row j0-1), v on half
-// rows j0-1..j0+R (local 0..R+1), columns i0-1..i0+W (local 0..W+1).
-template <typename T>
-__device__ void tile_derive(const MemberDev<T>& md, TileSmem<T>& t, bool u_halo_row = false, bool given = false) {
+// After the copies: iap gd, then u on full rows j0..j0+R (local 1..R+1;
+// from local 0 when the stencil also needs row j0-1), v on half rows
+// j0-1..j0+R (local 0..R+1), columns i0-1..i0+W (local 0..W+1).
+template <typename T, int R, int W>
+__device__ void tile_derive(const MemberDev<T>& md, Tile<T, R, W>& t, bool u_halo_row = false,
+                            bool given = false) {
+  using TL = Tile<T, R, W>;
   const int M = md.M, Mh = md.Mh;
-  const int SW = t.SW, n = t.rows * SW;
   cp_async_wait_all();
   __syncthreads();
-  for (int p = threadIdx.x; p < n; p += blockDim.x) t.ig[p] = sqrt(t.gd[p]);
+  for (int p = threadIdx.x; p < TL::NS; p += kThreads) t.ig[p] = sqrt(t.gd[p]);
   __syncthreads();
   if (given) return;
   const int urow0 = u_halo_row ? 0 : 1;
-  const int nd = (t.R + 2) * (t.W + 2);
-  for (int q = threadIdx.x; q < nd; q += blockDim.x) {
-    const int rr = q / (t.W + 2), cc = q - rr * (t.W + 2);
-    const int p = rr * SW + cc;
+  constexpr int DW = W + 2, ND = (R + 2) * (W + 2);
+  for (int q = threadIdx.x; q < ND; q += kThreads) {
+    const int rr = q / DW, cc = q - rr * DW;
+    const int p = TL::pos(rr, cc);
     const int j = t.j0 - 1 + rr;
+    const bool need = rr <= t.vrows + 1 && cc <= t.vcols + 1;
     T uu = 0, vv = 0;
-    if (rr >= urow0 && j >= 1 && j <= M - 2) uu = t.iu[p] * T(2) / (t.ig[p] + t.ig[p + 1]);
-    if (j >= 0 && j < Mh) vv = t.iv[p] * T(2) / (t.ig[p] + t.ig[p + SW]);
+    if (need && rr >= urow0 && j >= 1 && j <= M - 2) uu = t.iu[p] * T(2) / (t.ig[p] + t.ig[p + 1]);
+    if (need && j >= 0 && j < Mh) vv = t.iv[p] * T(2) / (t.ig[p] + t.ig[p + TL::SW]);
     t.u[p] = uu;
     t.v[p] = vv;
   }
@@ -238,10 +333,10 @@ __device__ inline void load_member(const MemberDev<T>* __restrict__ mems, int me
 // ----------------------------------------------------- point operators
 // p is the local position of full row j / half row j, column i.
 
-template <typename T, int PASS, int ADV>
-__device__ inline T point_du(const MemberDev<T>& md, const TileSmem<T>& t, int j, int p, T beta_lon,
+template <typename T, int PASS, int ADV, class TL>
+__device__ inline T point_du(const MemberDev<T>& md, const TL& t, int j, int p, T beta_lon,
                              T beta_lat) {
-  const int SW = t.SW;
+  constexpr int SW = TL::SW;
   T r = 0;
   if (PASS != kFastPass) {
     // src/dycore_mod.F90:376-392 / :393-415
@@ -249,31 +344,31 @@ __device__ inline T point_du(const MemberDev<T>& md, const TileSmem<T>& t, int j
     const T u1 = uc + um, u2 = uc + up;
     T adv_lon;
     if (ADV == GDC_ADV_CENTER_DIFF) {
-      adv_lon = cf(md, CF_RADVLON, j) * (u2 * t.iu[p + 1] - u1 * t.iu[p - 1]);
+      adv_lon = t.cf(TF_RADVLON, j) * (u2 * t.iu[p + 1] - u1 * t.iu[p - 1]);
     } else {
       const T ic = t.iu[p], ip = t.iu[p + 1], im = t.iu[p - 1];
-      adv_lon = cf(md, CF_RADVLON, j) * (u2 * (ic + ip) - beta_lon * fabs(u2) * (ip - ic) - u1 * (ic + im) +
+      adv_lon = t.cf(TF_RADVLON, j) * (u2 * (ic + ip) - beta_lon * fabs(u2) * (ip - ic) - u1 * (ic + im) +
                                          beta_lon * fabs(u1) * (ic - im) - (u2 - u1) * ic);
     }
     // src/dycore_mod.F90:433-439 / :450-459
-    const T v1 = (t.v[p - SW] + t.v[p - SW + 1]) * ch(md, CH_COS, j - 1);
-    const T v2 = (t.v[p] + t.v[p + 1]) * ch(md, CH_COS, j);
+    const T v1 = (t.v[p - SW] + t.v[p - SW + 1]) * t.ch(TH_COS, j - 1);
+    const T v2 = (t.v[p] + t.v[p + 1]) * t.ch(TH_COS, j);
     T adv_lat;
     if (ADV == GDC_ADV_CENTER_DIFF) {
-      adv_lat = cf(md, CF_RADVLAT, j) * (v2 * t.iu[p + SW] - v1 * t.iu[p - SW]);
+      adv_lat = t.cf(TF_RADVLAT, j) * (v2 * t.iu[p + SW] - v1 * t.iu[p - SW]);
     } else {
       const T ic = t.iu[p], ip = t.iu[p + SW], im = t.iu[p - SW];
-      adv_lat = cf(md, CF_RADVLAT, j) * (v2 * (ic + ip) - beta_lat * fabs(v2) * (ip - ic) - v1 * (ic + im) +
+      adv_lat = t.cf(TF_RADVLAT, j) * (v2 * (ic + ip) - beta_lat * fabs(v2) * (ip - ic) - v1 * (ic + im) +
                                          beta_lat * fabs(v1) * (ic - im) - (v2 - v1) * ic);
     }
     r = -adv_lon - adv_lat;
   }
   if (PASS != kSlowPass) {
     // src/dycore_mod.F90:485-493
-    const T fv = T(0.25) * (cf(md, CF_F, j) + cf(md, CF_C, j) * t.u[p]) *
-                 (cf(md, CF_C1, j) * (t.iv[p - SW] + t.iv[p - SW + 1]) + cf(md, CF_C2, j) * (t.iv[p] + t.iv[p + 1]));
+    const T fv = T(0.25) * (t.cf(TF_F, j) + t.cf(TF_C, j) * t.u[p]) *
+                 (t.cf(TF_C1, j) * (t.iv[p - SW] + t.iv[p - SW + 1]) + t.cf(TF_C2, j) * (t.iv[p] + t.iv[p + 1]));
     // src/dycore_mod.F90:514-519
-    const T pgf = T(0.5) * (t.ig[p] + t.ig[p + 1]) / cf(md, CF_DLON, j) *
+    const T pgf = T(0.5) * (t.ig[p] + t.ig[p + 1]) / t.cf(TF_DLON, j) *
                   (t.gd[p + 1] + t.ghs[p + 1] - t.gd[p] - t.ghs[p]);
     if (PASS == kAllPass)
       r = r + fv - pgf;
@@ -283,10 +378,10 @@ __device__ inline T point_du(const MemberDev<T>& md, const TileSmem<T>& t, int j
   return r;
 }
 
-template <typename T, int PASS, int ADV>
-__device__ inline T point_dv(const MemberDev<T>& md, const TileSmem<T>& t, int jh, int p, T beta_lon,
+template <typename T, int PASS, int ADV, class TL>
+__device__ inline T point_dv(const MemberDev<T>& md, const TL& t, int jh, int p, T beta_lon,
                              T beta_lat) {
-  const int SW = t.SW;
+  constexpr int SW = TL::SW;
   T r = 0;
   if (PASS != kFastPass) {
     // src/dycore_mod.F90:386-391 / :406-414
@@ -294,34 +389,34 @@ __device__ inline T point_dv(const MemberDev<T>& md, const TileSmem<T>& t, int j
     const T u2 = t.u[p] + t.u[p + SW];
     T adv_lon;
     if (ADV == GDC_ADV_CENTER_DIFF) {
-      adv_lon = ch(md, CH_RADVLON, jh) * (u2 * t.iv[p + 1] - u1 * t.iv[p - 1]);
+      adv_lon = t.ch(TH_RADVLON, jh) * (u2 * t.iv[p + 1] - u1 * t.iv[p - 1]);
     } else {
       const T ic = t.iv[p], ip = t.iv[p + 1], im = t.iv[p - 1];
-      adv_lon = ch(md, CH_RADVLON, jh) * (u2 * (ic + ip) - beta_lon * fabs(u2) * (ip - ic) - u1 * (ic + im) +
+      adv_lon = t.ch(TH_RADVLON, jh) * (u2 * (ic + ip) - beta_lon * fabs(u2) * (ip - ic) - u1 * (ic + im) +
                                           beta_lon * fabs(u1) * (ic - im) - (u2 - u1) * ic);
     }
     // src/dycore_mod.F90:441-446 / :461-469
-    const T vc = t.v[p] * ch(md, CH_COS, jh);
-    const T v1 = vc + t.v[p - SW] * ch(md, CH_COS, jh - 1);
-    const T v2 = vc + t.v[p + SW] * ch(md, CH_COS, jh + 1);
+    const T vc = t.v[p] * t.ch(TH_COS, jh);
+    const T v1 = vc + t.v[p - SW] * t.ch(TH_COS, jh - 1);
+    const T v2 = vc + t.v[p + SW] * t.ch(TH_COS, jh + 1);
     T adv_lat;
     if (ADV == GDC_ADV_CENTER_DIFF) {
-      adv_lat = ch(md, CH_RADVLAT, jh) * (v2 * t.iv[p + SW] - v1 * t.iv[p - SW]);
+      adv_lat = t.ch(TH_RADVLAT, jh) * (v2 * t.iv[p + SW] - v1 * t.iv[p - SW]);
     } else {
       const T ic = t.iv[p], ip = t.iv[p + SW], im = t.iv[p - SW];
-      adv_lat = ch(md, CH_RADVLAT, jh) * (v2 * (ic + ip) - beta_lat * fabs(v2) * (ip - ic) - v1 * (ic + im) +
+      adv_lat = t.ch(TH_RADVLAT, jh) * (v2 * (ic + ip) - beta_lat * fabs(v2) * (ip - ic) - v1 * (ic + im) +
                                           beta_lat * fabs(v1) * (ic - im) - (v2 - v1) * ic);
     }
     r = -adv_lon - adv_lat;
   }
   if (PASS != kSlowPass) {
     // src/dycore_mod.F90:495-503
-    const T f0 = cf(md, CF_F, jh), c0 = cf(md, CF_C, jh);
-    const T f1 = cf(md, CF_F, jh + 1), c1 = cf(md, CF_C, jh + 1);
+    const T f0 = t.cf(TF_F, jh), c0 = t.cf(TF_C, jh);
+    const T f1 = t.cf(TF_F, jh + 1), c1 = t.cf(TF_C, jh + 1);
     const T fu = T(0.25) * ((f0 + c0 * t.u[p]) * t.iu[p] + (f0 + c0 * t.u[p - 1]) * t.iu[p - 1] +
                             (f1 + c1 * t.u[p + SW]) * t.iu[p + SW] + (f1 + c1 * t.u[p + SW - 1]) * t.iu[p + SW - 1]);
     // src/dycore_mod.F90:530-535
-    const T pgf = T(0.5) * (t.ig[p] + t.ig[p + SW]) / ch(md, CH_DLAT, jh) * ch(md, CH_COS, jh) *
+    const T pgf = T(0.5) * (t.ig[p] + t.ig[p + SW]) / t.ch(TH_DLAT, jh) * t.ch(TH_COS, jh) *
                   (t.gd[p + SW] + t.ghs[p + SW] - t.gd[p] - t.ghs[p]);
     if (PASS == kAllPass)
       r = r - fu - pgf;
@@ -332,17 +427,17 @@ __device__ inline T point_dv(const MemberDev<T>& md, const TileSmem<T>& t, int j
 }
 
 // Interior rows only (1..M-2); pole rows come from the zonal-sum cap.
-template <typename T, int PASS>
-__device__ inline T point_dgd(const MemberDev<T>& md, const TileSmem<T>& t, int j, int p) {
+template <typename T, int PASS, class TL>
+__device__ inline T point_dgd(const MemberDev<T>& md, const TL& t, int j, int p) {
   if (PASS == kSlowPass) return T(0);  // src/dycore_mod.F90:297
-  const int SW = t.SW;
+  constexpr int SW = TL::SW;
   // src/dycore_mod.F90:546-552
   const T mdlon = ((t.ig[p] + t.ig[p + 1]) * t.iu[p] - (t.ig[p] + t.ig[p - 1]) * t.iu[p - 1]) * T(0.5) /
-                  cf(md, CF_DLON, j);
+                  t.cf(TF_DLON, j);
   // src/dycore_mod.F90:564-570
-  const T mdlat = ((t.ig[p] + t.ig[p + SW]) * t.iv[p] * ch(md, CH_COS, j) -
-                   (t.ig[p] + t.ig[p - SW]) * t.iv[p - SW] * ch(md, CH_COS, j - 1)) *
-                  T(0.5) / cf(md, CF_DLAT, j);
+  const T mdlat = ((t.ig[p] + t.ig[p + SW]) * t.iv[p] * t.ch(TH_COS, j) -
+                   (t.ig[p] + t.ig[p - SW]) * t.iv[p - SW] * t.ch(TH_COS, j - 1)) *
+                  T(0.5) / t.cf(TF_DLAT, j);
   return -mdlon - mdlat;
 }
 
@@ -466,7 +561,7 @@ struct StageOcc {
   static constexpr int kMinBlocks = sizeof(T) == 4 ? 4 : 2;
 };
 
-template <typename T, int PASS, int ADV>
+template <typename T, int PASS, int ADV, int R, int W>
 __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
     stage_kernel(const MemberDev<T>* __restrict__ mems, const WorkItem* __restrict__ wl, StageArgs a,
                  int staging_words, int max_n) {
@@ -496,22 +591,23 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
 
   if (w.kind == 0) {
     // ---------------- bulk tile: rows j0..j0+R-1 are ordinary rows
-    TileSmem<T> t = carve_tile(staging, w.rows, w.cols, w.j0, w.i0);
+    using TL = Tile<T, R, W>;
+    constexpr int PPT = (R * W + kThreads - 1) / kThreads;
+    TL t = carve<T, R, W>(staging, w.j0, w.i0, w.rows, w.cols);
     tile_issue(md, gd_in, iu_in, iv_in, t, given);
     // While the tile is in flight, fetch the per-point update operands.
-    const int npts = w.rows * w.cols;
     const bool base_in_tile = a.out_slot >= 0 && a.base_slot == a.in_slot;
-    T pre_b[kPPT][3], pre_p[kPPT][3];
+    T pre_b[PPT][3], pre_p[PPT][3];
 #pragma unroll
-    for (int k = 0; k < kPPT; ++k) {
+    for (int k = 0; k < PPT; ++k) {
       const int q = threadIdx.x + k * kThreads;
 #pragma unroll
       for (int f = 0; f < 3; ++f) {
         pre_b[k][f] = T(0);
         pre_p[k][f] = T(0);
       }
-      if (q < npts) {
-        const int r = q / w.cols, c = q - r * w.cols;
+      const int r = q / W, c = q - r * W;
+      if (q < R * W && r < w.rows && c < w.cols) {
         const size_t o = (size_t)(w.j0 + r) * N + (w.i0 + c);
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
@@ -522,12 +618,12 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
     }
     tile_derive(md, t, false, given);
 #pragma unroll
-    for (int k = 0; k < kPPT; ++k) {
+    for (int k = 0; k < PPT; ++k) {
       const int q = threadIdx.x + k * kThreads;
-      if (q >= npts) break;
-      const int r = q / w.cols, c = q - r * w.cols;
+      const int r = q / W, c = q - r * W;
+      if (q >= R * W || r >= w.rows || c >= w.cols) continue;
       const int j = w.j0 + r, i = w.i0 + c;
-      const int p = (r + 1) * t.SW + (c + 1);
+      const int p = TL::pos(r + 1, c + 1);
       const size_t o = (size_t)j * N + i;
       if (base_in_tile) {
         pre_b[k][F_GD] = t.gd[p];
@@ -538,13 +634,13 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
       const T dv = point_dv<T, PASS, ADV>(md, t, j, p, ub_lon, ub_lat);
       const T dg = point_dgd<T, PASS>(md, t, j, p);
       if (plain_ops) {
-        em.put(F_IU, o, du, cf(md, CF_COS, j), pre_b[k][F_IU], pre_p[k][F_IU]);
-        em.put(F_IV, o, dv, ch(md, CH_COS, j), pre_b[k][F_IV], pre_p[k][F_IV]);
-        em.put(F_GD, o, dg, cf(md, CF_COS, j), pre_b[k][F_GD], pre_p[k][F_GD]);
+        em.put(F_IU, o, du, t.cf(TF_COS, j), pre_b[k][F_IU], pre_p[k][F_IU]);
+        em.put(F_IV, o, dv, t.ch(TH_COS, j), pre_b[k][F_IV], pre_p[k][F_IV]);
+        em.put(F_GD, o, dg, t.cf(TF_COS, j), pre_b[k][F_GD], pre_p[k][F_GD]);
       } else {
-        em.put(F_IU, o, du, cf(md, CF_COS, j), em.base_of(F_IU, o), em.prev_of(F_IU, o));
-        em.put(F_IV, o, dv, ch(md, CH_COS, j), em.base_of(F_IV, o), em.prev_of(F_IV, o));
-        em.put(F_GD, o, dg, cf(md, CF_COS, j), em.base_of(F_GD, o), em.prev_of(F_GD, o));
+        em.put(F_IU, o, du, t.cf(TF_COS, j), em.base_of(F_IU, o), em.prev_of(F_IU, o));
+        em.put(F_IV, o, dv, t.ch(TH_COS, j), em.base_of(F_IV, o), em.prev_of(F_IV, o));
+        em.put(F_GD, o, dg, t.cf(TF_COS, j), em.base_of(F_GD, o), em.prev_of(F_GD, o));
       }
     }
   } else {
@@ -558,14 +654,15 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
     T* rdv = rows + max_n;
     T* rdg = rows + 2 * max_n;
     Acc<double> cap;
+    using TR = Tile<T, 1, kRowChunk>;
     for (int c0 = 0; c0 < N; c0 += kRowChunk) {
-      const int W = min(kRowChunk, N - c0);
-      TileSmem<T> t = carve_tile(staging, 1, W, j, c0);
+      const int vw = min(kRowChunk, N - c0);
+      TR t = carve<T, 1, kRowChunk>(staging, j, c0, 1, vw);
       __syncthreads();
       tile_issue(md, gd_in, iu_in, iv_in, t, given);
       tile_derive(md, t, false, given);
-      for (int c = threadIdx.x; c < W; c += blockDim.x) {
-        const int p = t.SW + (c + 1);
+      for (int c = threadIdx.x; c < vw; c += blockDim.x) {
+        const int p = TR::pos(1, c + 1);
         const int i = c0 + c;
         rdu[i] = has_du ? point_du<T, PASS, ADV>(md, t, j, p, ub_lon, ub_lat) : T(0);
         rdv[i] = has_dv ? point_dv<T, PASS, ADV>(md, t, j, p, ub_lon, ub_lat) : T(0);
@@ -574,9 +671,9 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
           // np -= (ig(j)+ig(j-1)) iv(j-1).  Terms and sum in FP64.
           if (PASS != kSlowPass) {
             if (south)
-              cap.add(((double)t.ig[p] + (double)t.ig[p + t.SW]) * (double)t.iv[p]);
+              cap.add(((double)t.ig[p] + (double)t.ig[p + TR::SW]) * (double)t.iv[p]);
             else
-              cap.add(((double)t.ig[p] + (double)t.ig[p - t.SW]) * (double)t.iv[p - t.SW]);
+              cap.add(((double)t.ig[p] + (double)t.ig[p - TR::SW]) * (double)t.iv[p - TR::SW]);
           }
           rdg[i] = T(0);
         } else {
@@ -731,7 +828,7 @@ __global__ void __launch_bounds__(kThreads)
   const MemberDev<T>& md = smd;
   const int N = md.N, M = md.M, Mh = md.Mh;
   const double* dc = md.dcoef;
-  Acc<double> mass, en;
+  typename DiagAcc<T>::type mass, en;
   auto point = [&](int j, int i, bool hv) {
     const size_t o = (size_t)j * N + i;
     const double g = val64(md, a.slot, F_GD, o);
@@ -757,8 +854,8 @@ __global__ void __launch_bounds__(kThreads)
   } else {
     for (int i = threadIdx.x; i < N; i += blockDim.x) point(w.j0, i, w.j0 <= Mh - 1);
   }
-  const Acc<double> sm = block_acc(mass, red);
-  const Acc<double> se = block_acc(en, red);
+  const auto sm = block_acc(mass, red);
+  const auto se = block_acc(en, red);
   if (threadIdx.x == 0) {
     double* pp = a.partials + 4 * (size_t)w.pidx;
     pp[0] = sm.s;
@@ -805,35 +902,36 @@ __device__ inline T lap_lon(const T* f, int p, T d) {
   return (f[p + 1] - T(2) * f[p] + f[p - 1]) / (d * d);
 }
 
-template <typename T>
-__device__ inline T point_gdd_like(const MemberDev<T>& md, const TileSmem<T>& t, const T* f, int j, int p) {
+template <typename T, class TL>
+__device__ inline T point_gdd_like(const MemberDev<T>& md, const TL& t, const T* f, int j, int p) {
   // src/diffusion_mod.F90:109-115 (and :135-143 for u)
-  const int SW = t.SW;
-  const T dl = cf(md, CF_DLAT, j);
-  return lap_lon(f, p, cf(md, CF_DLON, j)) +
-         ((f[p + SW] - f[p]) * ch(md, CH_COS, j) - (f[p] - f[p - SW]) * ch(md, CH_COS, j - 1)) / (dl * dl) *
-             cf(md, CF_COS, j);
+  constexpr int SW = TL::SW;
+  const T dl = t.cf(TF_DLAT, j);
+  return lap_lon(f, p, t.cf(TF_DLON, j)) +
+         ((f[p + SW] - f[p]) * t.ch(TH_COS, j) - (f[p] - f[p - SW]) * t.ch(TH_COS, j - 1)) / (dl * dl) *
+             t.cf(TF_COS, j);
 }
 
-template <typename T>
-__device__ inline T point_vd(const MemberDev<T>& md, const TileSmem<T>& t, int jh, int p) {
+template <typename T, class TL>
+__device__ inline T point_vd(const MemberDev<T>& md, const TL& t, int jh, int p) {
   // src/diffusion_mod.F90:145-171
-  const int SW = t.SW, Mh = md.Mh;
+  constexpr int SW = TL::SW;
+  const int Mh = md.Mh;
   const T* v = t.v;
-  T vd = lap_lon(v, p, ch(md, CH_DLON, jh));
-  const T dl = ch(md, CH_DLAT, jh);
+  T vd = lap_lon(v, p, t.ch(TH_DLON, jh));
+  const T dl = t.ch(TH_DLAT, jh);
   if (jh >= 1 && jh <= Mh - 2) {
-    vd = vd + ((v[p + SW] - v[p]) * cf(md, CF_COS, jh + 1) - (v[p] - v[p - SW]) * cf(md, CF_COS, jh)) / (dl * dl) *
-                  ch(md, CH_COS, jh);
+    vd = vd + ((v[p + SW] - v[p]) * t.cf(TF_COS, jh + 1) - (v[p] - v[p - SW]) * t.cf(TF_COS, jh)) / (dl * dl) *
+                  t.ch(TH_COS, jh);
   } else if (jh == 0) {
-    vd = vd + (v[p + SW] - v[p]) * cf(md, CF_COS, jh + 1) / (dl * dl) * ch(md, CH_COS, jh);
+    vd = vd + (v[p + SW] - v[p]) * t.cf(TF_COS, jh + 1) / (dl * dl) * t.ch(TH_COS, jh);
   } else {
-    vd = vd - (v[p] - v[p - SW]) * cf(md, CF_COS, jh) / (dl * dl) * ch(md, CH_COS, jh);
+    vd = vd - (v[p] - v[p - SW]) * t.cf(TF_COS, jh) / (dl * dl) * t.ch(TH_COS, jh);
   }
   return vd;
 }
 
-template <typename T>
+template <typename T, int R, int W>
 __global__ void __launch_bounds__(kThreads)
     diffusion_lap_kernel(const MemberDev<T>* __restrict__ mems, const WorkItem* __restrict__ wl, int slot, double c,
                          int staging_words, int max_n) {
@@ -854,14 +952,15 @@ __global__ void __launch_bounds__(kThreads)
   T* vo = md.st[SL_SA][F_IV];
   const T cc_ = T(c);
   if (w.kind == 0) {
-    TileSmem<T> t = carve_tile(staging, w.rows, w.cols, w.j0, w.i0);
+    using TL = Tile<T, R, W>;
+    TL t = carve<T, R, W>(staging, w.j0, w.i0, w.rows, w.cols);
     tile_issue(md, gd_in, md.st[slot][F_IU], md.st[slot][F_IV], t);
     tile_derive(md, t, true);
     const int npts = w.rows * w.cols;
     for (int q = threadIdx.x; q < npts; q += blockDim.x) {
       const int r = q / w.cols, cl = q - r * w.cols;
       const int j = w.j0 + r, i = w.i0 + cl;
-      const int p = (r + 1) * t.SW + (cl + 1);
+      const int p = TL::pos(r + 1, cl + 1);
       const size_t o = (size_t)j * N + i;
       go[o] = t.gd[p] + cc_ * point_gdd_like(md, t, t.gd, j, p);
       uo[o] = t.u[p] + cc_ * point_gdd_like(md, t, t.u, j, p);
@@ -877,24 +976,25 @@ __global__ void __launch_bounds__(kThreads)
     T* ru = rows + max_n;
     T* rv = rows + 2 * max_n;
     Acc<double> cap;
+    using TR = Tile<T, 1, kRowChunk>;
     for (int c0 = 0; c0 < N; c0 += kRowChunk) {
-      const int W = min(kRowChunk, N - c0);
-      TileSmem<T> t = carve_tile(staging, 1, W, j, c0);
+      const int vw = min(kRowChunk, N - c0);
+      TR t = carve<T, 1, kRowChunk>(staging, j, c0, 1, vw);
       __syncthreads();
       tile_issue(md, gd_in, md.st[slot][F_IU], md.st[slot][F_IV], t);
       tile_derive(md, t, true);
-      for (int cl = threadIdx.x; cl < W; cl += blockDim.x) {
-        const int p = t.SW + (cl + 1);
+      for (int cl = threadIdx.x; cl < vw; cl += blockDim.x) {
+        const int p = TR::pos(1, cl + 1);
         const int i = c0 + cl;
         if (pole) {
           // sp = sp + gd(i,j+1) - gd(i,j); np = np - (gd(i,j) - gd(i,j-1)):
           // the terms +gd(j+1), -gd(j) (south) and -gd(j), +gd(j-1) (north).
           if (j == 0) {
-            cap.add((double)t.gd[p + t.SW]);
+            cap.add((double)t.gd[p + TR::SW]);
             cap.add(-(double)t.gd[p]);
           } else {
             cap.add(-(double)t.gd[p]);
-            cap.add((double)t.gd[p - t.SW]);
+            cap.add((double)t.gd[p - TR::SW]);
           }
           rg[i] = T(0);
         } else {
@@ -1015,8 +1115,11 @@ static inline int check_launch() {
 
 template <typename T>
 size_t stage_smem_bytes(int tile_rows, int tile_cols, int max_n, int* staging_words) {
-  const int bulk = 7 * (tile_rows + 3) * (tile_cols + 3);
-  const int row = 7 * 4 * (kRowChunk + 3);
+  int bulk = 0;
+  if (tile_rows == 8 && tile_cols == 32) bulk = tile_words<T, 8, 32>();
+  if (tile_rows == 8 && tile_cols == 64) bulk = tile_words<T, 8, 64>();
+  if (tile_rows == 4 && tile_cols == 128) bulk = tile_words<T, 4, 128>();
+  const int row = tile_words<T, 1, kRowChunk>();
   // Rounded to 4 words and max_n to an even count so that the FP64
   // reduction buffer after the T arrays stays 8-byte aligned.
   const int sw = ((bulk > row ? bulk : row) + 3) & ~3;
@@ -1025,31 +1128,28 @@ size_t stage_smem_bytes(int tile_rows, int tile_cols, int max_n, int* staging_wo
   return (size_t)(sw + 3 * max_n + kMaxKeep + 64) * sizeof(T) + 64 * sizeof(double) + 16;
 }
 
-template <typename T, int PASS, int ADV>
-static int launch_stage_t(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int tile_rows, int tile_cols,
-                          int max_n, const StageArgs& a, cudaStream_t s) {
+template <typename T, int PASS, int ADV, int R, int W>
+static int launch_stage_t(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int max_n, const StageArgs& a,
+                          cudaStream_t s) {
   int sw = 0;
   max_n = (max_n + 1) & ~1;
-  const size_t smem = stage_smem_bytes<T>(tile_rows, tile_cols, max_n, &sw);
+  const size_t smem = stage_smem_bytes<T>(R, W, max_n, &sw);
   static size_t configured = 0;
   if (smem > configured) {
-    if (cudaFuncSetAttribute(stage_kernel<T, PASS, ADV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-        cudaSuccess)
+    if (cudaFuncSetAttribute(stage_kernel<T, PASS, ADV, R, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess)
       return check_launch();
     configured = smem;
   }
-  stage_kernel<T, PASS, ADV><<<nwork, kThreads, smem, s>>>(mem, wl, a, sw, max_n);
+  stage_kernel<T, PASS, ADV, R, W><<<nwork, kThreads, smem, s>>>(mem, wl, a, sw, max_n);
   return check_launch();
 }
 
-template <typename T>
-int launch_stage(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int adv, int tile_rows, int tile_cols,
-                 int max_n, const StageArgs& a, void* stream) {
-  if (nwork <= 0) return GDC_OK;
-  if (tile_rows * tile_cols > kPPT * kThreads) return GDC_E_CONFIG;
-  cudaStream_t s = (cudaStream_t)stream;
+template <typename T, int R, int W>
+static int launch_stage_shape(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int adv, int max_n,
+                              const StageArgs& a, cudaStream_t s) {
 #define GDC_DISPATCH(P, A) \
-  if (a.pass == P && adv == A) return launch_stage_t<T, P, A>(mem, wl, nwork, tile_rows, tile_cols, max_n, a, s);
+  if (a.pass == P && adv == A) return launch_stage_t<T, P, A, R, W>(mem, wl, nwork, max_n, a, s);
   GDC_DISPATCH(kAllPass, GDC_ADV_CENTER_DIFF)
   GDC_DISPATCH(kFastPass, GDC_ADV_CENTER_DIFF)
   GDC_DISPATCH(kSlowPass, GDC_ADV_CENTER_DIFF)
@@ -1057,6 +1157,17 @@ int launch_stage(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int adv
   GDC_DISPATCH(kFastPass, GDC_ADV_UPWIND)
   GDC_DISPATCH(kSlowPass, GDC_ADV_UPWIND)
 #undef GDC_DISPATCH
+  return GDC_E_CONFIG;
+}
+
+template <typename T>
+int launch_stage(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int adv, int tile_rows, int tile_cols,
+                 int max_n, const StageArgs& a, void* stream) {
+  if (nwork <= 0) return GDC_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (tile_rows == 8 && tile_cols == 32) return launch_stage_shape<T, 8, 32>(mem, wl, nwork, adv, max_n, a, s);
+  if (tile_rows == 8 && tile_cols == 64) return launch_stage_shape<T, 8, 64>(mem, wl, nwork, adv, max_n, a, s);
+  if (tile_rows == 4 && tile_cols == 128) return launch_stage_shape<T, 4, 128>(mem, wl, nwork, adv, max_n, a, s);
   return GDC_E_CONFIG;
 }
 
@@ -1095,13 +1206,20 @@ int launch_diffusion(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int
   max_n = (max_n + 1) & ~1;
   const size_t smem = stage_smem_bytes<T>(tile_rows, tile_cols, max_n, &sw);
   static size_t configured = 0;
+  auto lap = diffusion_lap_kernel<T, 8, 32>;
+  if (tile_rows == 8 && tile_cols == 64)
+    lap = diffusion_lap_kernel<T, 8, 64>;
+  else if (tile_rows == 4 && tile_cols == 128)
+    lap = diffusion_lap_kernel<T, 4, 128>;
+  else if (!(tile_rows == 8 && tile_cols == 32))
+    return GDC_E_CONFIG;
   if (smem > configured) {
-    if (cudaFuncSetAttribute(diffusion_lap_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-        cudaSuccess)
-      return check_launch();
+    for (auto k : {diffusion_lap_kernel<T, 8, 32>, diffusion_lap_kernel<T, 8, 64>, diffusion_lap_kernel<T, 4, 128>})
+      if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return check_launch();
     configured = smem;
   }
-  diffusion_lap_kernel<T><<<nwork, kThreads, smem, s>>>(mem, wl, slot, sign_dt_coef, sw, max_n);
+  lap<<<nwork, kThreads, smem, s>>>(mem, wl, slot, sign_dt_coef, sw, max_n);
   int rc = check_launch();
   if (rc != GDC_OK) return rc;
   diffusion_iap_kernel<T><<<nwork, kThreads, 0, s>>>(mem, wl, slot, uvslot);

@@ -65,8 +65,10 @@ extern "C" int gdc_tendency_noalloc(const gdc_params* p, int pass, const double*
   if (p->uv_adv_scheme != GDC_ADV_CENTER_DIFF && p->uv_adv_scheme != GDC_ADV_UPWIND)
     return fail(GDC_E_CONFIG, "gdc_tendency_noalloc: uv_adv_scheme must be center_diff or upwind");
   const int N = p->num_lon, M = p->num_lat, Mh = M - 1;
-  if (N < 8 || M < 5 || N > 1440 || M > 721)
-    return fail(GDC_E_CONFIG, "gdc_tendency_noalloc: grid must be within 8..1440 x 5..721 (scratch is 2 MiB)");
+  if (N < 8 || M < 5 || N > 1440 || M > 721 || N % 4 != 0)
+    return fail(GDC_E_CONFIG,
+                "gdc_tendency_noalloc: grid must be within 8..1440 x 5..721 with num_lon a multiple of 4 "
+                "(scratch is 2 MiB)");
   for (int k = 0; k < 20; ++k) {
     const int c = p->zonal_tend_filter_cutoff_wavenumber[k];
     if (c < 0 || 2 * (c + 1) >= N || 2 * (c + 1) > 120)

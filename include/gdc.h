@@ -98,7 +98,8 @@ int gdc_steps_for_run(const gdc_params* p);
 typedef struct gdc_handle gdc_handle;
 
 /* dycore_init (src/dycore_mod.F90:60-111): mesh, coefficients, filter
- * masks, device buffers.  Reads no state. */
+ * masks, device buffers.  Reads no state.  num_lon must be a multiple of 4
+ * (every grid of the reference's test suite is). */
 int gdc_create(const gdc_params* p, gdc_handle** out);
 /* dycore_final (src/dycore_mod.F90:144-157). */
 void gdc_destroy(gdc_handle* h);
@@ -243,8 +244,8 @@ int gdc_batch_diag(gdc_batch* b, int member_id, double* total_mass,
 /* Number of active (admitted, unfinished) members. */
 int gdc_batch_active(gdc_batch* b, int* n_active);
 
-/* Tile shape of the stage kernels: rows x columns per work item; 0,0 picks
- * the tuned default.  gdc_batch_autotune times the candidates on the
+/* Tile shape of the stage kernels: rows x columns per work item, one of
+ * 8x32, 8x64, 4x128 (compiled shapes); 0,0 picks the default.  gdc_batch_autotune times the candidates on the
  * current members and keeps the fastest; the chosen shape is returned. */
 int gdc_batch_set_tile(gdc_batch* b, int tile_rows, int tile_cols);
 int gdc_batch_autotune(gdc_batch* b, int* tile_rows, int* tile_cols,

@@ -63,3 +63,26 @@ def test_fp32_compensated_vs_fp64(native):
         out[prec] = m.get_state()
     e = [rel_l2(a, b) for a, b in zip(out[gdc.FP32], out[gdc.FP64])]
     assert e[2] <= 1e-5, e
+
+
+@pytest.mark.parametrize("tile", [(8, 32), (8, 64), (4, 128)])
+def test_every_tile_shape_matches_oracle_on_ragged_grid(native, tile):
+    """720 columns leave a ragged last column block under every tile shape
+    (16, 16 and 80 columns), whose halo columns wrap to 0 and 1."""
+    from oracle.oracle import OracleModel
+    N, M = 720, 361
+    p = scheme(gdc, N, M, 120.0, subcycles=2, cutoff=(4,) * 5)
+    ic = gdc.ic_seeded(N, M, seed=5)
+    b = gdc.Batch(p)
+    b.set_tile(*tile)
+    mid = b.add(N, M, 120.0, 1, *ic)
+    b.step(1)
+    b.sync()
+    got = b.get_state(mid)
+    b.close()
+    o = OracleModel.from_params(p)
+    o.set_state(*ic)
+    o.step(1)
+    ref = o.get_state()
+    for name, a in zip(("u", "v", "gd"), got):
+        assert np.array_equal(interior(a), interior(ref[name])), (tile, name)
