@@ -34,7 +34,7 @@ bool uses_isp(const gdc_params& p) { return p.split_scheme == GDC_SPLIT_ISP; }
 
 // Byte layout of one member's device allocation.
 struct Layout {
-  size_t st[SL_N][3], lo[SL_N][3], td[TS_N][3], ghs, coef, twid, rowinfo, dcoef, given_u, given_v, total;
+  size_t st[SL_N][3], lo[SL_N][3], td[TS_N][3], ghs, coef, rowc, twid, rowinfo, dcoef, given_u, given_v, total;
 };
 
 template <typename T>
@@ -61,6 +61,7 @@ Layout make_layout(const gdc_params& p, int N, int M) {
       L.td[t][f] = (t <= TS_NEW || isp) ? take(fsz[f] * sizeof(T)) : (size_t)-1;
   L.ghs = take(full * sizeof(T));
   L.coef = take(coef_words(M) * sizeof(T));
+  L.rowc = take(rec_words(M) * sizeof(T));
   L.twid = take(2 * (size_t)N * sizeof(T));
   L.rowinfo = take((size_t)M * sizeof(int));
   L.dcoef = take((size_t)(3 * M) * sizeof(double));
@@ -126,6 +127,9 @@ class Batch final : public BatchIface {
     cudaError_t e = cudaSetDevice(P.device);
     if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("cudaSetDevice", e));
     e = cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming);
     if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("cudaStreamCreate", e));
     stream = own_stream;
     if (int rc = dalloc((void**)&d_mem, sizeof(MemberDev<T>) * kSlots)) return rc;
@@ -143,8 +147,7 @@ class Batch final : public BatchIface {
     recs.resize(kSlots);
     hdesc.resize(kSlots);
     std::memset(hdesc.data(), 0, sizeof(MemberDev<T>) * kSlots);
-    tile_r = 8;
-    tile_c = default_cols();
+    set_tile(0, 0);
     e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("init", e));
     return GDC_OK;
@@ -180,7 +183,7 @@ class Batch final : public BatchIface {
         break;
       }
     if (slot < 0) return fail(GDC_E_OOM, "add: member table full");
-    const Layout L = make_layout<T>(P, N, M);
+    const Layout L = make_layout<T>(mp, N, M);
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
     if (free_b < L.total + reserve) return fail(GDC_E_OOM, "add: not enough free device memory");
@@ -224,6 +227,7 @@ class Batch final : public BatchIface {
       coef[ch_off(CH_DLON, M) + j + 1] = T(co.half_dlon[j]);
       coef[ch_off(CH_DLAT, M) + j + 1] = T(co.half_dlat[j]);
     }
+    const std::vector<T> rowc = row_records(coef, M);
     std::vector<T> twid(2 * (size_t)N);
     for (int k = 0; k < N; ++k) {
       twid[k] = T(std::cos(2.0 * kPi * k / N));
@@ -288,6 +292,7 @@ class Batch final : public BatchIface {
       for (int f = 0; f < 3; ++f) d.td[t][f] = L.td[t][f] == (size_t)-1 ? nullptr : (T*)(base + L.td[t][f]);
     d.ghs = (T*)(base + L.ghs);
     d.coef = (const T*)(base + L.coef);
+    d.rowc = (const T*)(base + L.rowc);
     d.twid = (const T*)(base + L.twid);
     d.rowinfo = (const int*)(base + L.rowinfo);
     d.dcoef = (const double*)(base + L.dcoef);
@@ -297,6 +302,7 @@ class Batch final : public BatchIface {
     sync_stream();
     e = cudaMemset(r.dmem, 0, L.total);
     if (e == cudaSuccess) e = cudaMemcpy(base + L.coef, coef.data(), coef.size() * sizeof(T), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(base + L.rowc, rowc.data(), rowc.size() * sizeof(T), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(base + L.twid, twid.data(), twid.size() * sizeof(T), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(base + L.rowinfo, r.rowinfo.data(), M * sizeof(int), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(base + L.dcoef, dco.data(), dco.size() * sizeof(double), cudaMemcpyHostToDevice);
@@ -510,13 +516,16 @@ class Batch final : public BatchIface {
 
   int set_tile(int r, int c) override {
     if (r == 0 && c == 0) {
-      r = 8;
+      r = default_rows();
       c = default_cols();
     }
-    if (!tile_shape_supported(r, c))
-      return fail(GDC_E_CONFIG, "set_tile: supported shapes are 8x32, 8x64 and 4x128");
+    const bool st = strip_shape_supported(r, c);
+    if (!st && !tile_shape_supported(r, c))
+      return fail(GDC_E_CONFIG,
+                  "set_tile: supported shapes are tiles 8x32, 8x64, 4x128 and warp strips 8x30, 16x30, 32x30, 64x30");
     tile_r = r;
     tile_c = c;
+    strips = st;
     dirty = true;
     return GDC_OK;
   }
@@ -531,7 +540,7 @@ class Batch final : public BatchIface {
   // Times each candidate tile shape on the current members (graph replay,
   // CUDA events) and keeps the fastest.  Advances the members.
   int autotune(int* rr, int* cc, double* best_ms) override {
-    static const int cand[][2] = {{8, 32}, {8, 64}, {4, 128}};
+    static const int cand[][2] = {{8, 32}, {8, 64}, {4, 128}, {16, 30}, {32, 30}};
     double best = 1e30;
     int br = tile_r, bc = tile_c;
     for (auto& c : cand) {
@@ -620,8 +629,15 @@ class Batch final : public BatchIface {
     StageArgs a = base_args(pass);
     a.in_slot = level_of(id);
     a.tout = TS_NEW;
-    int rc = launch_stage<T>(d_mem, dwl, (int)wl.size(), P.uv_adv_scheme, tile_r, tile_c,
-                             std::max(max_n, N), a, stream);
+    int nr = 0;
+    for (const auto& w : wl) nr += w.kind == 1;
+    int rc = GDC_OK;
+    if (!strips)
+      rc = launch_stage<T>(d_mem, dwl, (int)wl.size(), P.uv_adv_scheme, tile_r, tile_c, std::max(max_n, N), a, stream);
+    else {
+      rc = launch_stage<T>(d_mem, dwl, nr, P.uv_adv_scheme, 8, 32, std::max(max_n, N), a, stream);
+      if (!rc) rc = launch_stage_strips<T>(d_mem, dwl + nr, (int)wl.size() - nr, P.uv_adv_scheme, a, stream);
+    }
     cudaError_t e = cudaStreamSynchronize(stream);
     cudaFree(dwl);
     if (rc) return fail(rc, "debug_tendency: launch failed");
@@ -661,6 +677,15 @@ class Batch final : public BatchIface {
   long long* d_nan = nullptr;
   WorkItem* d_wl = nullptr;
   size_t wl_cap = 0;
+  FlatItem* d_flat = nullptr;
+  size_t flat_cap = 0;
+  std::vector<FlatItem> hflat;
+  int nflat = 0;
+  FlatItem* d_dl = nullptr;      // diag items: rows of a member, one warp per row
+  double* d_dpart = nullptr;     // their partial sums
+  size_t dl_cap = 0;
+  std::vector<FlatItem> hdl;
+  int ndl = 0;
   double* d_partials = nullptr;
   size_t part_cap = 0;
   std::vector<MemberRec> recs;
@@ -668,16 +693,30 @@ class Batch final : public BatchIface {
   std::vector<WorkItem> hwl;
   std::vector<int> active_slots;
   int nwork = 0, max_n = 0;
-  int tile_r = 8, tile_c = 32;
+  int nrow = 0;                  // whole-row tasks at the head of the work list
+  int tile_r = 8, tile_c = 32;   // tile shape, or band rows x kStripCols
+  bool strips = false;           // work list of warp strips instead of tiles
+  // With strips, the whole-row tasks run on a second stream, concurrently
+  // with the strips over the ordinary rows.
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // Tile work list (8x32) for the diffusion and copy kernels when the stage
+  // kernels run on strips; otherwise the main list.
+  WorkItem* d_twl = nullptr;
+  size_t twl_cap = 0;
+  int ntwork = 0;
   int old_ = SL_L1, new_ = SL_L2;  // src/time_mod.F90:68-69
   bool dirty = true, warm = false, use_graph = true;
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
   std::vector<Prof> prof;
   std::vector<void*> allocs;
 
-  // FP32 is bandwidth-bound: larger tiles amortise the halo; FP64 is
-  // arithmetic-bound: smaller tiles spread the rows over more SMs.
+  // FP32: 8x64 tiles (fastest of the layouts on the 64-member ensemble);
+  // FP64 is arithmetic-bound: 8x32 tiles spread the rows over more SMs.
+  static int default_rows() { return 8; }
   static int default_cols() { return sizeof(T) == 4 ? 64 : 32; }
+
+  const WorkItem* tile_list() const { return strips ? d_twl : d_wl; }
 
   int fail(int code, const std::string& m) {
     err = m;
@@ -717,8 +756,15 @@ class Batch final : public BatchIface {
       if (r.dmem) cudaFree(r.dmem);
     for (void* p : allocs) cudaFree(p);
     if (d_wl) cudaFree(d_wl);
+    if (d_twl) cudaFree(d_twl);
+    if (d_flat) cudaFree(d_flat);
+    if (d_dl) cudaFree(d_dl);
+    if (d_dpart) cudaFree(d_dpart);
     if (d_partials) cudaFree(d_partials);
     if (own_stream) cudaStreamDestroy(own_stream);
+    if (side) cudaStreamDestroy(side);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
   }
 
   cudaError_t upload_field(T* dst, T* lo, const std::vector<double>& src) {
@@ -745,7 +791,23 @@ class Batch final : public BatchIface {
     return e;
   }
 
+  // Diag items of member s: bands of kDiagRows rows.
+  void append_diag_items(int s, std::vector<FlatItem>& out) {
+    hdesc[s].dbase = (int)out.size();
+    for (int j = 0; j < recs[s].M; j += kDiagRows)
+      out.push_back(FlatItem{s, 0, j, std::min(kDiagRows, recs[s].M - j)});
+    hdesc[s].dcount = (int)out.size() - hdesc[s].dbase;
+  }
+
   void append_items(int s, std::vector<WorkItem>& out, int& pcount) {
+    append_items_as(s, out, pcount, strips, tile_r, tile_c, true);
+  }
+
+  // Work items of member s: its whole-row tasks, then tiles (tr x tc) or
+  // warp strips (bands of tr rows, kStripCols columns) over its runs of
+  // ordinary rows.
+  void append_items_as(int s, std::vector<WorkItem>& out, int& pcount, bool as_strips, int tr, int tc,
+                       bool own_partials) {
     const MemberRec& r = recs[s];
     const int N = r.N, M = r.M;
     int pbase = pcount;
@@ -761,15 +823,23 @@ class Batch final : public BatchIface {
       }
       int b = j;
       while (b + 1 < M && !(r.rowinfo[b + 1] & RI_SPECIAL)) ++b;
-      for (int j0 = j; j0 <= b; j0 += tile_r) {
-        const int rows = std::min(tile_r, b - j0 + 1);
-        for (int i0 = 0; i0 < N; i0 += tile_c)
-          out.push_back(WorkItem{s, 0, j0, i0, rows, std::min(tile_c, N - i0), pcount++, 0});
+      if (as_strips) {
+        for (int i0 = 0; i0 < N; i0 += kStripCols)
+          for (int j0 = j; j0 <= b; j0 += tr)
+            out.push_back(WorkItem{s, 2, j0, i0, std::min(tr, b - j0 + 1), std::min(kStripCols, N - i0), pcount++, 0});
+      } else {
+        for (int j0 = j; j0 <= b; j0 += tr) {
+          const int rows = std::min(tr, b - j0 + 1);
+          for (int i0 = 0; i0 < N; i0 += tc)
+            out.push_back(WorkItem{s, 0, j0, i0, rows, std::min(tc, N - i0), pcount++, 0});
+        }
       }
       j = b + 1;
     }
-    hdesc[s].pbase = pbase;
-    hdesc[s].pcount = pcount - pbase;
+    if (own_partials) {  // the stage list's partial slots of this member
+      hdesc[s].pbase = pbase;
+      hdesc[s].pcount = pcount - pbase;
+    }
   }
 
   int rebuild() {
@@ -784,12 +854,61 @@ class Batch final : public BatchIface {
       active_slots.push_back(s);
       std::vector<WorkItem> items;
       append_items(s, items, pc);
-      for (auto& w : items) (w.kind ? rows_first : tiles).push_back(w);
+      for (auto& w : items) (w.kind == 1 ? rows_first : tiles).push_back(w);
       max_n = std::max(max_n, recs[s].N);
     }
     hwl = rows_first;
     hwl.insert(hwl.end(), tiles.begin(), tiles.end());
     nwork = (int)hwl.size();
+    nrow = (int)rows_first.size();
+    std::vector<WorkItem> htwl;
+    if (strips) {
+      int pt = 0;
+      std::vector<WorkItem> trows, ttiles;
+      for (int s : active_slots) {
+        std::vector<WorkItem> items;
+        append_items_as(s, items, pt, false, 8, 32, false);
+        for (auto& w : items) (w.kind == 1 ? trows : ttiles).push_back(w);
+      }
+      htwl = trows;
+      htwl.insert(htwl.end(), ttiles.begin(), ttiles.end());
+    }
+    ntwork = strips ? (int)htwl.size() : nwork;
+    hflat.clear();
+    for (int s : active_slots) {
+      const int n[3] = {recs[s].N * recs[s].M, recs[s].N * recs[s].M, recs[s].N * (recs[s].M - 1)};
+      for (int f = 0; f < 3; ++f)
+        for (int b = 0; b < n[f]; b += flat_chunk<T>())
+          hflat.push_back(FlatItem{s, f, b, std::min(flat_chunk<T>(), n[f] - b)});
+    }
+    nflat = (int)hflat.size();
+    hdl.clear();
+    for (int s : active_slots) append_diag_items(s, hdl);
+    ndl = (int)hdl.size();
+    if ((size_t)ndl > dl_cap) {
+      if (d_dl) cudaFree(d_dl);
+      if (d_dpart) cudaFree(d_dpart);
+      d_dl = nullptr;
+      d_dpart = nullptr;
+      dl_cap = std::max<size_t>(ndl, 2 * dl_cap);
+      cudaError_t e = cudaMalloc(&d_dl, dl_cap * sizeof(FlatItem));
+      if (e == cudaSuccess) e = cudaMalloc(&d_dpart, dl_cap * 4 * sizeof(double));
+      if (e != cudaSuccess) return fail(GDC_E_OOM, cuda_msg("rebuild: diag list", e));
+    }
+    if ((size_t)nflat > flat_cap) {
+      if (d_flat) cudaFree(d_flat);
+      d_flat = nullptr;
+      flat_cap = std::max<size_t>(nflat, 2 * flat_cap);
+      cudaError_t e = cudaMalloc(&d_flat, flat_cap * sizeof(FlatItem));
+      if (e != cudaSuccess) return fail(GDC_E_OOM, cuda_msg("rebuild: flat list", e));
+    }
+    if (strips && (size_t)ntwork > twl_cap) {
+      if (d_twl) cudaFree(d_twl);
+      d_twl = nullptr;
+      twl_cap = std::max<size_t>(ntwork, 2 * twl_cap);
+      cudaError_t e = cudaMalloc(&d_twl, twl_cap * sizeof(WorkItem));
+      if (e != cudaSuccess) return fail(GDC_E_OOM, cuda_msg("rebuild: tile list", e));
+    }
     if ((size_t)nwork > wl_cap) {
       if (d_wl) cudaFree(d_wl);
       d_wl = nullptr;
@@ -806,6 +925,11 @@ class Batch final : public BatchIface {
     }
     cudaError_t e = cudaSuccess;
     if (nwork) e = cudaMemcpy(d_wl, hwl.data(), nwork * sizeof(WorkItem), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && strips && ntwork)
+      e = cudaMemcpy(d_twl, htwl.data(), ntwork * sizeof(WorkItem), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && nflat)
+      e = cudaMemcpy(d_flat, hflat.data(), nflat * sizeof(FlatItem), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && ndl) e = cudaMemcpy(d_dl, hdl.data(), ndl * sizeof(FlatItem), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && !active_slots.empty())
       e = cudaMemcpy(d_active, active_slots.data(), active_slots.size() * sizeof(int), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(d_mem, hdesc.data(), sizeof(MemberDev<T>) * kSlots, cudaMemcpyHostToDevice);
@@ -842,7 +966,21 @@ class Batch final : public BatchIface {
       cudaEventCreate(&e1);
       cudaEventRecord(e0, stream);
     }
-    int rc = launch_stage<T>(d_mem, d_wl, nwork, P.uv_adv_scheme, tile_r, tile_c, max_n, a, stream);
+    int rc = GDC_OK;
+    if (!strips) {
+      rc = launch_stage<T>(d_mem, d_wl, nwork, P.uv_adv_scheme, tile_r, tile_c, max_n, a, stream);
+    } else if (pr) {  // timed launch by launch: one stream
+      rc = launch_stage<T>(d_mem, d_wl, nrow, P.uv_adv_scheme, 8, 32, max_n, a, stream);
+      if (!rc) rc = launch_stage_strips<T>(d_mem, d_wl + nrow, nwork - nrow, P.uv_adv_scheme, a, stream);
+    } else {
+      // whole-row tasks on the side stream, strips on the main stream
+      cudaEventRecord(ev_fork, stream);
+      cudaStreamWaitEvent(side, ev_fork, 0);
+      rc = launch_stage<T>(d_mem, d_wl, nrow, P.uv_adv_scheme, 8, 32, max_n, a, side);
+      if (!rc) rc = launch_stage_strips<T>(d_mem, d_wl + nrow, nwork - nrow, P.uv_adv_scheme, a, stream);
+      cudaEventRecord(ev_join, side);
+      cudaStreamWaitEvent(stream, ev_join, 0);
+    }
     if (pr) {
       cudaEventRecord(e1, stream);
       pr->push_back(Prof{0, e0, e1});
@@ -871,7 +1009,7 @@ class Batch final : public BatchIface {
       cudaEventCreate(&e1);
       cudaEventRecord(e0, stream);
     }
-    int rc = launch_final<T>(d_mem, d_wl, nwork, a, stream);
+    int rc = launch_final<T>(d_mem, d_flat, nflat, a, stream);
     if (pr) {
       cudaEventRecord(e1, stream);
       pr->push_back(Prof{1, e0, e1});
@@ -914,7 +1052,7 @@ class Batch final : public BatchIface {
   // isp_splitting (src/dycore_mod.F90:689-752).
   int isp(std::vector<Prof>* pr) {
     const int m = P.subcycles;
-    if (int rc = launch_copy_state<T>(d_mem, d_wl, nwork, old_, SL_SAVED, stream))
+    if (int rc = launch_copy_state<T>(d_mem, tile_list(), ntwork, old_, SL_SAVED, stream))
       return fail(rc, "copy launch failed");
     StageArgs a = base_args(kSlowPass);
     a.in_slot = old_;
@@ -999,7 +1137,8 @@ class Batch final : public BatchIface {
         cudaEventCreate(&e1);
         cudaEventRecord(e0, stream);
       }
-      rc = launch_diffusion<T>(d_mem, d_wl, nwork, tile_r, tile_c, max_n, new_, c, d_uvslot, stream);
+      rc = launch_diffusion<T>(d_mem, tile_list(), ntwork, strips ? 8 : tile_r, strips ? 32 : tile_c, max_n, new_, c,
+                               d_uvslot, stream);
       if (pr) {
         cudaEventRecord(e1, stream);
         pr->push_back(Prof{3, e0, e1});
@@ -1010,7 +1149,7 @@ class Batch final : public BatchIface {
     DiagArgs d;
     d.slot = new_;
     d.count_step = 1;
-    d.partials = d_partials;
+    d.partials = d_dpart;
     d.diag = d_diag;
     d.beta = d_beta;
     d.steps = d_steps;
@@ -1021,7 +1160,7 @@ class Batch final : public BatchIface {
       cudaEventCreate(&e1);
       cudaEventRecord(e0, stream);
     }
-    rc = launch_diag<T>(d_mem, d_wl, nwork, d_active, (int)active_slots.size(), d, stream);
+    rc = launch_diag<T>(d_mem, d_dl, ndl, d_active, (int)active_slots.size(), d, stream);
     if (pr) {
       cudaEventRecord(e1, stream);
       pr->push_back(Prof{2, e0, e1});
@@ -1031,14 +1170,13 @@ class Batch final : public BatchIface {
 
   // diag_run of a freshly admitted member's initial state.
   int initial_diag(int slot) {
-    std::vector<WorkItem> wl;
-    int pc = 0;
+    std::vector<FlatItem> wl;
     const MemberDev<T> saved = hdesc[slot];
-    append_items(slot, wl, pc);
-    WorkItem* dwl = nullptr;
+    append_diag_items(slot, wl);
+    FlatItem* dwl = nullptr;
     double* dpart = nullptr;
     int* dslot = nullptr;
-    if (cudaMalloc(&dwl, sizeof(WorkItem) * wl.size()) != cudaSuccess ||
+    if (cudaMalloc(&dwl, sizeof(FlatItem) * wl.size()) != cudaSuccess ||
         cudaMalloc(&dpart, sizeof(double) * 4 * wl.size()) != cudaSuccess ||
         cudaMalloc(&dslot, sizeof(int)) != cudaSuccess) {
       cudaGetLastError();
@@ -1046,9 +1184,9 @@ class Batch final : public BatchIface {
       if (dpart) cudaFree(dpart);
       return fail(GDC_E_OOM, "initial diag: cudaMalloc");
     }
-    cudaMemcpy(dwl, wl.data(), sizeof(WorkItem) * wl.size(), cudaMemcpyHostToDevice);
-    cudaMemcpy(dslot, &slot, sizeof(int), cudaMemcpyHostToDevice);
-    cudaMemcpy(d_mem + slot, &hdesc[slot], sizeof(MemberDev<T>), cudaMemcpyHostToDevice);
+    cudaError_t e = cudaMemcpy(dwl, wl.data(), sizeof(FlatItem) * wl.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dslot, &slot, sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_mem + slot, &hdesc[slot], sizeof(MemberDev<T>), cudaMemcpyHostToDevice);
     DiagArgs d;
     d.slot = old_;
     d.count_step = 0;  // the initial diag is not a step
@@ -1057,14 +1195,15 @@ class Batch final : public BatchIface {
     d.beta = nullptr;
     d.steps = d_steps;
     d.nan_step = d_nan;
-    int rc = launch_diag<T>(d_mem, dwl, (int)wl.size(), dslot, 1, d, stream);
-    cudaError_t e = cudaStreamSynchronize(stream);
+    int rc = e == cudaSuccess ? launch_diag<T>(d_mem, dwl, (int)wl.size(), dslot, 1, d, stream) : GDC_E_CUDA;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     cudaFree(dwl);
     cudaFree(dpart);
     cudaFree(dslot);
-    hdesc[slot].pbase = saved.pbase;
-    hdesc[slot].pcount = saved.pcount;
-    if (rc || e != cudaSuccess) return fail(GDC_E_CUDA, "initial diag failed");
+    hdesc[slot].dbase = saved.dbase;
+    hdesc[slot].dcount = saved.dcount;
+    if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("initial diag", e));
+    if (rc) return fail(rc, "initial diag: launch failed");
     return GDC_OK;
   }
 

@@ -72,6 +72,31 @@ inline size_t coef_words(int M) { return (size_t)CF_NFULL * M + (size_t)CH_NHALF
 GDC_HD inline size_t cf_off(int k, int M) { return (size_t)k * M; }
 GDC_HD inline size_t ch_off(int k, int M) { return (size_t)CF_NFULL * M + (size_t)k * (M + 1); }
 
+// Per-row coefficient records for the stencil tiles: record j+1 holds, for
+// row j = -1..M, the full-row coefficients of row j in TileFull order and
+// the half-row coefficients of half row j in TileHalf order, 16 words per
+// record so that a tile copies its rows 16 bytes at a time.  Entries of rows
+// outside the tables are 0.0, as in the table above.
+enum TileFull { TF_RADVLON, TF_RADVLAT, TF_F, TF_C, TF_C1, TF_C2, TF_DLON, TF_DLAT, TF_COS, TF_N };
+enum TileHalf { TH_COS = TF_N, TH_RADVLON, TH_RADVLAT, TH_DLAT, TH_DLON, TH_END };
+constexpr int kRecWords = 16;
+static_assert(TH_END <= kRecWords, "coefficient record overflow");
+inline size_t rec_words(int M) { return (size_t)(M + 2) * kRecWords; }
+template <typename T>
+std::vector<T> row_records(const std::vector<T>& coef, int M) {
+  static const int fsrc[TF_N] = {CF_RADVLON, CF_RADVLAT, CF_F, CF_C, CF_C1, CF_C2, CF_DLON, CF_DLAT, CF_COS};
+  static const int hsrc[TH_END - TH_COS] = {CH_COS, CH_RADVLON, CH_RADVLAT, CH_DLAT, CH_DLON};
+  std::vector<T> rec(rec_words(M), T(0));
+  for (int j = -1; j <= M; ++j) {
+    T* r = rec.data() + (size_t)(j + 1) * kRecWords;
+    if (j >= 0 && j < M)
+      for (int k = 0; k < TF_N; ++k) r[k] = coef[cf_off(fsrc[k], M) + j];
+    if (j >= -1 && j <= M - 1)
+      for (int k = 0; k < TH_END - TH_COS; ++k) r[TH_COS + k] = coef[ch_off(hsrc[k], M) + j + 1];
+  }
+  return rec;
+}
+
 // Row information bits (per row index j = 0..M-1).
 enum RowBits {
   RI_SPECIAL = 1,    // handled by a whole-row task (pole or filtered row)
@@ -93,7 +118,8 @@ template <typename T>
 struct MemberDev {
   int N, M, Mh;
   int pbase, pcount;      // partial-sum slots of this member's work items
-  int pad0;
+  int dbase, dcount;      // partial-sum slots of this member's diag items
+  int pad0, pad1;
   double pcdt[3];         // predict_correct time_step_size per Pass
   double dt;              // time_step_size
   T* st[SL_N][3];         // state slots: gd, iap u, iap v
@@ -101,6 +127,7 @@ struct MemberDev {
   T* td[TS_N][3];         // tendency slots: dgd, du, dv
   T* ghs;
   const T* coef;
+  const T* rowc;          // coefficient records of rows -1..M (kRecWords each)
   const T* twid;          // cos(2 pi m/N), m<N, then sin(2 pi m/N)
   const int* rowinfo;
   const double* dcoef;    // FP64 diag weights: mass weight [M], full cos [M], half cos [Mh]
@@ -145,7 +172,43 @@ struct StageArgs {
   double ub_lon, ub_lat;             // uv_adv_upwind_{lon,lat}_beta
   double rescale_rtol;               // gdc_params::filter_rescale_rtol
   int* uvslot;                       // per member: slot whose u, v are given (-1 none)
+  int form;                          // UpdateForm, set by the launchers
 };
+
+// Warp strips: output columns per warp (lanes 1..30 of the 32), and the
+// band heights (rows marched by one warp) the engine offers.
+constexpr int kStripCols = 30;
+
+// Update forms the bulk tiles specialise (the three stages of
+// predict_correct); anything else takes the general path.
+enum UpdateForm {
+  UF_PREDICT_IN = 0,   // out = in + h T                    (base is the input level)
+  UF_PREDICT_OUT = 1,  // out = base + h T, tout = T
+  UF_CORRECT = 2,      // tout = T, inner products with tprev
+  UF_GENERAL = 3,
+};
+inline int update_form(const StageArgs& a) {
+  const bool plain = a.taccum < 0 && a.tadd < 0 && a.tadd2 < 0;
+  if (!plain) return UF_GENERAL;
+  if (a.out_slot >= 0 && a.base_slot == a.in_slot && a.tout < 0 && !a.do_ip) return UF_PREDICT_IN;
+  if (a.out_slot >= 0 && a.base_slot != a.in_slot && a.tout >= 0 && !a.do_ip) return UF_PREDICT_OUT;
+  if (a.out_slot < 0 && a.tout >= 0 && a.do_ip && a.beta_mode == 0 && a.tprev >= 0) return UF_CORRECT;
+  return UF_GENERAL;
+}
+
+// A contiguous run of one field of one member: elements [begin, begin+count)
+// of the field's array (gd, iap u: M rows; iap v: M-1 rows; N per row).
+struct FlatItem {
+  int member;
+  int field;
+  int begin;
+  int count;
+};
+// Elements per flat item: 4 16-byte vectors per thread of a 256-thread block.
+template <typename T>
+GDC_HD constexpr int flat_chunk() {
+  return 256 * 4 * (16 / (int)sizeof(T));
+}
 
 struct FinalArgs {
   int base_slot, out_slot, tslot;
@@ -166,22 +229,26 @@ struct DiagArgs {
   long long* nan_step;   // per member: first step with NaN mass/energy
 };
 
-// Tile shapes compiled for the stage and diffusion kernels (rows x columns).
+// Tile shapes compiled for the stage and diffusion kernels (rows x columns),
+// and the warp-strip layouts of the stage kernel (band rows x kStripCols).
 inline bool tile_shape_supported(int r, int c) {
   return (r == 8 && c == 32) || (r == 8 && c == 64) || (r == 4 && c == 128);
 }
+inline bool strip_shape_supported(int r, int c) { return c == kStripCols && (r == 8 || r == 16 || r == 32 || r == 64); }
 
 // Kernel launchers (gdc_kernels_f64.cu / gdc_kernels_f32.cu).
 template <typename T>
 int launch_stage(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int adv, int tile_rows,
                  int tile_cols, int max_n, const StageArgs& a, void* stream);
 template <typename T>
-int launch_final(const MemberDev<T>* mem, const WorkItem* wl, int nwork, const FinalArgs& a,
+int launch_final(const MemberDev<T>* mem, const FlatItem* fl, int nflat, const FinalArgs& a,
                  void* stream);
 // Per-item partial sums, then one block per member (`slots`) forms the totals.
 template <typename T>
-int launch_diag(const MemberDev<T>* mem, const WorkItem* wl, int nwork, const int* slots,
+int launch_diag(const MemberDev<T>* mem, const FlatItem* dl, int ndl, const int* slots,
                 int nmembers, const DiagArgs& a, void* stream);
+// Rows per diag item (one warp per row).
+constexpr int kDiagRows = 8;
 // beta of each member in `slots` from the stage kernel's partials.
 template <typename T>
 int launch_beta(const MemberDev<T>* mem, const int* slots, int nmembers, const double* partials,
@@ -195,6 +262,11 @@ int launch_diffusion(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int
 template <typename T>
 int launch_copy_state(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int from_slot,
                       int to_slot, void* stream);
+// Warp strips of one stage (one warp per item; ordinary rows only: the
+// whole-row tasks go to launch_stage).
+template <typename T>
+int launch_stage_strips(const MemberDev<T>* mem, const WorkItem* strips, int nstrip, int adv, const StageArgs& a,
+                        void* stream);
 // Shared-memory bytes of one stage launch.
 template <typename T>
 size_t stage_smem_bytes(int tile_rows, int tile_cols, int max_n, int* staging_words);

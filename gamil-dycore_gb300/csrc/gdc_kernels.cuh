@@ -38,6 +38,9 @@ namespace gdc {
 
 constexpr int kThreads = 256;
 constexpr int kRowChunk = 128;  // columns per chunk of a whole-row task
+#ifndef GDC_STRIP_BLOCKS
+#define GDC_STRIP_BLOCKS 2  // resident strip blocks per SM (FP32)
+#endif
 constexpr int kMaxKeep = 128;   // packed FFT coefficients a filter row may keep
 
 // ------------------------------------------------------------ helpers
@@ -61,11 +64,22 @@ struct Acc<double> {
   }
   __device__ double value() const { return s + c; }
 };
+// FP32 sums are compensated too: beta = ip1 / ip2 differs from 1 by about
+// the step's relative change (1e-6), so a plain FP32 sum (relative error
+// ~1e-7 per block) would put percent-level errors on beta - 1.
 template <>
 struct Acc<float> {
   float s = 0, c = 0;
-  __device__ void add(float x) { s += x; }
-  __device__ void merge(float os, float oc) { s += os + oc; }
+  __device__ void add(float x) {
+    const float t = s + x;
+    const float bp = t - s;
+    c += (s - (t - bp)) + (x - bp);
+    s = t;
+  }
+  __device__ void merge(float os, float oc) {
+    add(os);
+    c += oc;
+  }
   __device__ float value() const { return s + c; }
 };
 
@@ -165,8 +179,8 @@ __device__ inline T ch(const MemberDev<T>& md, int k, int jh) {  // jh in -1..Mh
 // the derived iap gd, u and v.  Rows are padded so that column i0 starts on
 // a 16-byte boundary (the row interiors are copied 16 bytes at a time).
 // Partial tiles (the last row band of a run, the last column block of a
-// row) stage only what their valid points use.  `cfull` / `chalf` hold the
-// row coefficients of full rows j0-1..j0+R and half rows j0-1..j0+R.
+// row) stage only what their valid points use.  `rc` holds the coefficient
+// records of rows j0-1..j0+R (full row j and half row j in each).
 template <typename T, int R_, int W_>
 struct Tile {
   static constexpr int R = R_, W = W_;
@@ -176,23 +190,16 @@ struct Tile {
   static constexpr int ROWS = R_ + 3, NS = ROWS * SW;
   static constexpr int CR = R_ + 2;                // coefficient rows
   T *gd, *ghs, *iu, *iv, *ig, *u, *v;
-  T *cfull, *chalf;
+  T* rc;
   int j0, i0, vrows, vcols;
   __device__ static int pos(int rr, int cc) { return rr * SW + cc + OFF; }
-  __device__ T cf(int k, int j) const { return cfull[k * CR + (j - j0 + 1)]; }
-  __device__ T ch(int k, int jh) const { return chalf[k * CR + (jh - j0 + 1)]; }
+  __device__ T cf(int k, int j) const { return rc[(j - j0 + 1) * kRecWords + k]; }
+  __device__ T ch(int k, int jh) const { return rc[(jh - j0 + 1) * kRecWords + k]; }
 };
-
-// Full-row coefficients a tile reads, and the half-row ones.
-enum TileFull { TF_RADVLON, TF_RADVLAT, TF_F, TF_C, TF_C1, TF_C2, TF_DLON, TF_DLAT, TF_COS, TF_N };
-enum TileHalf { TH_COS, TH_RADVLON, TH_RADVLAT, TH_DLAT, TH_DLON, TH_N };
-__device__ __constant__ const int kTileFullSrc[TF_N] = {CF_RADVLON, CF_RADVLAT, CF_F, CF_C, CF_C1,
-                                                        CF_C2, CF_DLON, CF_DLAT, CF_COS};
-__device__ __constant__ const int kTileHalfSrc[TH_N] = {CH_COS, CH_RADVLON, CH_RADVLAT, CH_DLAT, CH_DLON};
 
 template <typename T, int R, int W>
 constexpr int tile_words() {
-  return 7 * Tile<T, R, W>::NS + (TF_N + TH_N) * Tile<T, R, W>::CR;
+  return 7 * Tile<T, R, W>::NS + kRecWords * Tile<T, R, W>::CR;
 }
 
 template <typename T, int R, int W>
@@ -206,8 +213,7 @@ __device__ inline Tile<T, R, W> carve(T* base, int j0, int i0, int vrows, int vc
   t.ig = base + 4 * n;
   t.u = base + 5 * n;
   t.v = base + 6 * n;
-  t.cfull = base + 7 * n;
-  t.chalf = t.cfull + TF_N * Tile<T, R, W>::CR;
+  t.rc = base + 7 * n;
   t.j0 = j0;
   t.i0 = i0;
   t.vrows = vrows;
@@ -277,17 +283,13 @@ __device__ void tile_issue(const MemberDev<T>& md, const T* __restrict__ gd, con
     }
   }
   (void)nfield;
-  // row coefficients of full rows j0-1..j0+R and half rows j0-1..j0+R
-  for (int q = threadIdx.x; q < (TF_N + TH_N) * TL::CR; q += kThreads) {
-    const int k = q / TL::CR, lr = q - k * TL::CR;
+  // coefficient records of rows j0-1..j0+R (records exist for rows -1..M)
+  constexpr int RCH = kRecWords / VEC;  // 16-byte copies per record
+  for (int q = threadIdx.x; q < TL::CR * RCH; q += kThreads) {
+    const int lr = q / RCH, k = q - lr * RCH;
     const int j = t.j0 - 1 + lr;
-    T val = T(0);
-    if (k < TF_N) {
-      if (j >= 0 && j < M) val = md.coef[cf_off(kTileFullSrc[k], M) + j];
-    } else if (j >= -1 && j <= Mh) {
-      val = md.coef[ch_off(kTileHalfSrc[k - TF_N], M) + j + 1];
-    }
-    t.cfull[q] = val;  // cfull and chalf are contiguous
+    if (j > M) continue;  // beyond a partial tile: never read
+    cp_async16(&t.rc[lr * kRecWords + k * VEC], md.rowc + (size_t)(j + 1) * kRecWords + k * VEC, true);
   }
 }
 
@@ -333,43 +335,61 @@ __device__ inline void load_member(const MemberDev<T>* __restrict__ mems, int me
 // ----------------------------------------------------- point operators
 // p is the local position of full row j / half row j, column i.
 
-template <typename T, int PASS, int ADV, class TL>
-__device__ inline T point_du(const MemberDev<T>& md, const TL& t, int j, int p, T beta_lon,
-                             T beta_lat) {
-  constexpr int SW = TL::SW;
+// Stencil views: s.f(dr, dc) is field f at row offset dr and column offset
+// dc (-1..1) from the point, s.cf / s.ch the row coefficients, s.j the row.
+// TileView reads a shared-memory tile; the strip kernel has its own view
+// over registers.  The point operators below are written once for both.
+template <typename T, class TL>
+struct TileView {
+  const TL& t;
+  int p, j;
+  __device__ __forceinline__ T u(int dr, int dc) const { return t.u[p + dr * TL::SW + dc]; }
+  __device__ __forceinline__ T v(int dr, int dc) const { return t.v[p + dr * TL::SW + dc]; }
+  __device__ __forceinline__ T iu(int dr, int dc) const { return t.iu[p + dr * TL::SW + dc]; }
+  __device__ __forceinline__ T iv(int dr, int dc) const { return t.iv[p + dr * TL::SW + dc]; }
+  __device__ __forceinline__ T ig(int dr, int dc) const { return t.ig[p + dr * TL::SW + dc]; }
+  __device__ __forceinline__ T gd(int dr, int dc) const { return t.gd[p + dr * TL::SW + dc]; }
+  __device__ __forceinline__ T ghs(int dr, int dc) const { return t.ghs[p + dr * TL::SW + dc]; }
+  __device__ __forceinline__ T cf(int k, int jj) const { return t.cf(k, jj); }
+  __device__ __forceinline__ T ch(int k, int jj) const { return t.ch(k, jj); }
+};
+
+template <typename T, int PASS, int ADV, class S>
+__device__ __forceinline__ T point_du(const S& s, T beta_lon, T beta_lat) {
+  const int j = s.j;
   T r = 0;
   if (PASS != kFastPass) {
     // src/dycore_mod.F90:376-392 / :393-415
-    const T uc = t.u[p], um = t.u[p - 1], up = t.u[p + 1];
+    const T uc = s.u(0, 0), um = s.u(0, -1), up = s.u(0, 1);
     const T u1 = uc + um, u2 = uc + up;
     T adv_lon;
     if (ADV == GDC_ADV_CENTER_DIFF) {
-      adv_lon = t.cf(TF_RADVLON, j) * (u2 * t.iu[p + 1] - u1 * t.iu[p - 1]);
+      adv_lon = s.cf(TF_RADVLON, j) * (u2 * s.iu(0, 1) - u1 * s.iu(0, -1));
     } else {
-      const T ic = t.iu[p], ip = t.iu[p + 1], im = t.iu[p - 1];
-      adv_lon = t.cf(TF_RADVLON, j) * (u2 * (ic + ip) - beta_lon * fabs(u2) * (ip - ic) - u1 * (ic + im) +
+      const T ic = s.iu(0, 0), ip = s.iu(0, 1), im = s.iu(0, -1);
+      adv_lon = s.cf(TF_RADVLON, j) * (u2 * (ic + ip) - beta_lon * fabs(u2) * (ip - ic) - u1 * (ic + im) +
                                          beta_lon * fabs(u1) * (ic - im) - (u2 - u1) * ic);
     }
     // src/dycore_mod.F90:433-439 / :450-459
-    const T v1 = (t.v[p - SW] + t.v[p - SW + 1]) * t.ch(TH_COS, j - 1);
-    const T v2 = (t.v[p] + t.v[p + 1]) * t.ch(TH_COS, j);
+    const T v1 = (s.v(-1, 0) + s.v(-1, 1)) * s.ch(TH_COS, j - 1);
+    const T v2 = (s.v(0, 0) + s.v(0, 1)) * s.ch(TH_COS, j);
     T adv_lat;
     if (ADV == GDC_ADV_CENTER_DIFF) {
-      adv_lat = t.cf(TF_RADVLAT, j) * (v2 * t.iu[p + SW] - v1 * t.iu[p - SW]);
+      adv_lat = s.cf(TF_RADVLAT, j) * (v2 * s.iu(1, 0) - v1 * s.iu(-1, 0));
     } else {
-      const T ic = t.iu[p], ip = t.iu[p + SW], im = t.iu[p - SW];
-      adv_lat = t.cf(TF_RADVLAT, j) * (v2 * (ic + ip) - beta_lat * fabs(v2) * (ip - ic) - v1 * (ic + im) +
+      const T ic = s.iu(0, 0), ip = s.iu(1, 0), im = s.iu(-1, 0);
+      adv_lat = s.cf(TF_RADVLAT, j) * (v2 * (ic + ip) - beta_lat * fabs(v2) * (ip - ic) - v1 * (ic + im) +
                                          beta_lat * fabs(v1) * (ic - im) - (v2 - v1) * ic);
     }
     r = -adv_lon - adv_lat;
   }
   if (PASS != kSlowPass) {
     // src/dycore_mod.F90:485-493
-    const T fv = T(0.25) * (t.cf(TF_F, j) + t.cf(TF_C, j) * t.u[p]) *
-                 (t.cf(TF_C1, j) * (t.iv[p - SW] + t.iv[p - SW + 1]) + t.cf(TF_C2, j) * (t.iv[p] + t.iv[p + 1]));
+    const T fv = T(0.25) * (s.cf(TF_F, j) + s.cf(TF_C, j) * s.u(0, 0)) *
+                 (s.cf(TF_C1, j) * (s.iv(-1, 0) + s.iv(-1, 1)) + s.cf(TF_C2, j) * (s.iv(0, 0) + s.iv(0, 1)));
     // src/dycore_mod.F90:514-519
-    const T pgf = T(0.5) * (t.ig[p] + t.ig[p + 1]) / t.cf(TF_DLON, j) *
-                  (t.gd[p + 1] + t.ghs[p + 1] - t.gd[p] - t.ghs[p]);
+    const T pgf = T(0.5) * (s.ig(0, 0) + s.ig(0, 1)) / s.cf(TF_DLON, j) *
+                  (s.gd(0, 1) + s.ghs(0, 1) - s.gd(0, 0) - s.ghs(0, 0));
     if (PASS == kAllPass)
       r = r + fv - pgf;
     else
@@ -378,46 +398,45 @@ __device__ inline T point_du(const MemberDev<T>& md, const TL& t, int j, int p, 
   return r;
 }
 
-template <typename T, int PASS, int ADV, class TL>
-__device__ inline T point_dv(const MemberDev<T>& md, const TL& t, int jh, int p, T beta_lon,
-                             T beta_lat) {
-  constexpr int SW = TL::SW;
+template <typename T, int PASS, int ADV, class S>
+__device__ __forceinline__ T point_dv(const S& s, T beta_lon, T beta_lat) {
+  const int jh = s.j;
   T r = 0;
   if (PASS != kFastPass) {
     // src/dycore_mod.F90:386-391 / :406-414
-    const T u1 = t.u[p - 1] + t.u[p + SW - 1];
-    const T u2 = t.u[p] + t.u[p + SW];
+    const T u1 = s.u(0, -1) + s.u(1, -1);
+    const T u2 = s.u(0, 0) + s.u(1, 0);
     T adv_lon;
     if (ADV == GDC_ADV_CENTER_DIFF) {
-      adv_lon = t.ch(TH_RADVLON, jh) * (u2 * t.iv[p + 1] - u1 * t.iv[p - 1]);
+      adv_lon = s.ch(TH_RADVLON, jh) * (u2 * s.iv(0, 1) - u1 * s.iv(0, -1));
     } else {
-      const T ic = t.iv[p], ip = t.iv[p + 1], im = t.iv[p - 1];
-      adv_lon = t.ch(TH_RADVLON, jh) * (u2 * (ic + ip) - beta_lon * fabs(u2) * (ip - ic) - u1 * (ic + im) +
+      const T ic = s.iv(0, 0), ip = s.iv(0, 1), im = s.iv(0, -1);
+      adv_lon = s.ch(TH_RADVLON, jh) * (u2 * (ic + ip) - beta_lon * fabs(u2) * (ip - ic) - u1 * (ic + im) +
                                           beta_lon * fabs(u1) * (ic - im) - (u2 - u1) * ic);
     }
     // src/dycore_mod.F90:441-446 / :461-469
-    const T vc = t.v[p] * t.ch(TH_COS, jh);
-    const T v1 = vc + t.v[p - SW] * t.ch(TH_COS, jh - 1);
-    const T v2 = vc + t.v[p + SW] * t.ch(TH_COS, jh + 1);
+    const T vc = s.v(0, 0) * s.ch(TH_COS, jh);
+    const T v1 = vc + s.v(-1, 0) * s.ch(TH_COS, jh - 1);
+    const T v2 = vc + s.v(1, 0) * s.ch(TH_COS, jh + 1);
     T adv_lat;
     if (ADV == GDC_ADV_CENTER_DIFF) {
-      adv_lat = t.ch(TH_RADVLAT, jh) * (v2 * t.iv[p + SW] - v1 * t.iv[p - SW]);
+      adv_lat = s.ch(TH_RADVLAT, jh) * (v2 * s.iv(1, 0) - v1 * s.iv(-1, 0));
     } else {
-      const T ic = t.iv[p], ip = t.iv[p + SW], im = t.iv[p - SW];
-      adv_lat = t.ch(TH_RADVLAT, jh) * (v2 * (ic + ip) - beta_lat * fabs(v2) * (ip - ic) - v1 * (ic + im) +
+      const T ic = s.iv(0, 0), ip = s.iv(1, 0), im = s.iv(-1, 0);
+      adv_lat = s.ch(TH_RADVLAT, jh) * (v2 * (ic + ip) - beta_lat * fabs(v2) * (ip - ic) - v1 * (ic + im) +
                                           beta_lat * fabs(v1) * (ic - im) - (v2 - v1) * ic);
     }
     r = -adv_lon - adv_lat;
   }
   if (PASS != kSlowPass) {
     // src/dycore_mod.F90:495-503
-    const T f0 = t.cf(TF_F, jh), c0 = t.cf(TF_C, jh);
-    const T f1 = t.cf(TF_F, jh + 1), c1 = t.cf(TF_C, jh + 1);
-    const T fu = T(0.25) * ((f0 + c0 * t.u[p]) * t.iu[p] + (f0 + c0 * t.u[p - 1]) * t.iu[p - 1] +
-                            (f1 + c1 * t.u[p + SW]) * t.iu[p + SW] + (f1 + c1 * t.u[p + SW - 1]) * t.iu[p + SW - 1]);
+    const T f0 = s.cf(TF_F, jh), c0 = s.cf(TF_C, jh);
+    const T f1 = s.cf(TF_F, jh + 1), c1 = s.cf(TF_C, jh + 1);
+    const T fu = T(0.25) * ((f0 + c0 * s.u(0, 0)) * s.iu(0, 0) + (f0 + c0 * s.u(0, -1)) * s.iu(0, -1) +
+                            (f1 + c1 * s.u(1, 0)) * s.iu(1, 0) + (f1 + c1 * s.u(1, -1)) * s.iu(1, -1));
     // src/dycore_mod.F90:530-535
-    const T pgf = T(0.5) * (t.ig[p] + t.ig[p + SW]) / t.ch(TH_DLAT, jh) * t.ch(TH_COS, jh) *
-                  (t.gd[p + SW] + t.ghs[p + SW] - t.gd[p] - t.ghs[p]);
+    const T pgf = T(0.5) * (s.ig(0, 0) + s.ig(1, 0)) / s.ch(TH_DLAT, jh) * s.ch(TH_COS, jh) *
+                  (s.gd(1, 0) + s.ghs(1, 0) - s.gd(0, 0) - s.ghs(0, 0));
     if (PASS == kAllPass)
       r = r - fu - pgf;
     else
@@ -427,17 +446,17 @@ __device__ inline T point_dv(const MemberDev<T>& md, const TL& t, int jh, int p,
 }
 
 // Interior rows only (1..M-2); pole rows come from the zonal-sum cap.
-template <typename T, int PASS, class TL>
-__device__ inline T point_dgd(const MemberDev<T>& md, const TL& t, int j, int p) {
+template <typename T, int PASS, class S>
+__device__ __forceinline__ T point_dgd(const S& s) {
   if (PASS == kSlowPass) return T(0);  // src/dycore_mod.F90:297
-  constexpr int SW = TL::SW;
+  const int j = s.j;
   // src/dycore_mod.F90:546-552
-  const T mdlon = ((t.ig[p] + t.ig[p + 1]) * t.iu[p] - (t.ig[p] + t.ig[p - 1]) * t.iu[p - 1]) * T(0.5) /
-                  t.cf(TF_DLON, j);
+  const T mdlon = ((s.ig(0, 0) + s.ig(0, 1)) * s.iu(0, 0) - (s.ig(0, 0) + s.ig(0, -1)) * s.iu(0, -1)) * T(0.5) /
+                  s.cf(TF_DLON, j);
   // src/dycore_mod.F90:564-570
-  const T mdlat = ((t.ig[p] + t.ig[p + SW]) * t.iv[p] * t.ch(TH_COS, j) -
-                   (t.ig[p] + t.ig[p - SW]) * t.iv[p - SW] * t.ch(TH_COS, j - 1)) *
-                  T(0.5) / t.cf(TF_DLAT, j);
+  const T mdlat = ((s.ig(0, 0) + s.ig(1, 0)) * s.iv(0, 0) * s.ch(TH_COS, j) -
+                   (s.ig(0, 0) + s.ig(-1, 0)) * s.iv(-1, 0) * s.ch(TH_COS, j - 1)) *
+                  T(0.5) / s.cf(TF_DLAT, j);
   return -mdlon - mdlat;
 }
 
@@ -489,11 +508,14 @@ struct Emit {
 // 0..keep-1: a0, (a_k, b_k) for k <= cutoff, and a_(cutoff+1)) are
 // projected directly: forward sums by warps, reconstruction per point in
 // packed-index order.
+// `tw` holds the member's twiddles in shared memory: cos(2 pi m/N) at
+// tw[m], sin at tw[N + m] (copied by twiddles_to_shared).  Indices k n mod
+// N advance by additions.
 template <typename T>
-__device__ void filter_project(const MemberDev<T>& md, T* x, int keep, T* coefs) {
+__device__ void filter_project(const MemberDev<T>& md, T* x, int keep, T* coefs, const T* tw) {
   const int N = md.N;
-  const T* ctab = md.twid;
-  const T* stab = md.twid + N;
+  const T* ctab = tw;
+  const T* stab = tw + N;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   __syncthreads();
   for (int p = warp; p < keep; p += nw) {
@@ -503,7 +525,13 @@ __device__ void filter_project(const MemberDev<T>& md, T* x, int keep, T* coefs)
     } else {
       const int k = (p + 1) >> 1;
       const T* tab = (p & 1) ? ctab : stab;
-      for (int n = lane; n < N; n += 32) acc.add(x[n] * tab[(k * n) % N]);
+      const int step = (32 * k) % N;
+      int idx = (k * lane) % N;
+      for (int n = lane; n < N; n += 32) {
+        acc.add(x[n] * tab[idx]);
+        idx += step;
+        if (idx >= N) idx -= N;
+      }
     }
     warp_acc(acc);
     if (lane == 0) coefs[p] = acc.value() * (p == 0 ? T(1.0) / T(N) : T(2.0) / T(N));
@@ -511,12 +539,15 @@ __device__ void filter_project(const MemberDev<T>& md, T* x, int keep, T* coefs)
   __syncthreads();
   for (int n = threadIdx.x; n < N; n += blockDim.x) {
     T y = 0;
-    for (int p = 0; p < keep; ++p) {
-      if (p == 0) {
-        y = y + coefs[0];
+    y = y + coefs[0];
+    int idx = 0;  // k n mod N for the current k
+    for (int p = 1; p < keep; ++p) {
+      if (p & 1) {
+        idx += n;
+        if (idx >= N) idx -= N;
+        y = y + coefs[p] * ctab[idx];
       } else {
-        const int k = (p + 1) >> 1;
-        y = y + coefs[p] * ((p & 1) ? ctab : stab)[(k * n) % N];
+        y = y + coefs[p] * stab[idx];
       }
     }
     x[n] = y;
@@ -524,12 +555,18 @@ __device__ void filter_project(const MemberDev<T>& md, T* x, int keep, T* coefs)
   __syncthreads();
 }
 
+// Copy the member's twiddle tables (2N values) to shared memory.
+template <typename T>
+__device__ inline void twiddles_to_shared(const MemberDev<T>& md, T* tw) {
+  for (int i = threadIdx.x; i < 2 * md.N; i += blockDim.x) tw[i] = md.twid[i];
+}
+
 // The s1/s2-rescaled tendency filter of src/dycore_mod.F90:212-219.  With
 // rtol > 0 (an extension; 0 is the reference) the rescale is skipped when
 // s1 or s2 is zero to within rtol of the sum of the magnitudes of its terms.
 template <typename T>
 __device__ void filter_rescale(const MemberDev<T>& md, T* x, const T* __restrict__ w1, const T* __restrict__ w2,
-                               int keep, T* coefs, T* red, double rtol) {
+                               int keep, T* coefs, T* red, double rtol, const T* tw) {
   const int N = md.N;
   Acc<T> s, sa;
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
@@ -540,7 +577,7 @@ __device__ void filter_rescale(const MemberDev<T>& md, T* x, const T* __restrict
   const T s1 = block_value(s, red);
   const T a1 = rtol > 0 ? block_value(sa, red) : T(0);
   if (!(fabs(s1) > T(1.0e-16))) return;  // src/filter_mod.F90:31
-  filter_project(md, x, keep, coefs);
+  filter_project(md, x, keep, coefs, tw);
   Acc<T> q, qa;
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     const T t = x[i] * (w2 ? (w1[i] + w2[i]) : w1[i]);
@@ -556,6 +593,433 @@ __device__ void filter_rescale(const MemberDev<T>& md, T* x, const T* __restrict
 
 // --------------------------------------------------------- stage kernel
 
+// One bulk tile (rows j0..j0+rows-1, all ordinary; columns i0..i0+cols-1).
+// Thread t owns column t % W and RPT consecutive rows from (t / W) * RPT;
+// UF fixes the update form at compile time (UF_GENERAL: any StageArgs).
+template <typename T, int PASS, int ADV, int R, int W, int UF>
+__device__ __forceinline__ void bulk_tile(const MemberDev<T>& md, const StageArgs& a, const WorkItem& w,
+                                          T* staging, bool given, const T* gd_in, const T* iu_in,
+                                          const T* iv_in, T ub_lon, T ub_lat, Emit<T>& em) {
+  using TL = Tile<T, R, W>;
+  constexpr int RPT = R * W / kThreads;
+  static_assert(RPT * kThreads == R * W, "a tile is a whole number of rows per thread");
+  const int N = md.N;
+  TL t = carve<T, R, W>(staging, w.j0, w.i0, w.rows, w.cols);
+  tile_issue(md, gd_in, iu_in, iv_in, t, given);
+  const int c = threadIdx.x % W, r0 = (threadIdx.x / W) * RPT;
+  const bool cval = c < w.cols;
+  const int ob = (w.j0 + r0) * N + w.i0 + c;  // the thread's first point
+  // Operands fetched while the tile is in flight: the base level
+  // (predict 2) or the previous tendency (correct).
+  T pre[RPT][3];
+  if (UF == UF_PREDICT_OUT || UF == UF_CORRECT) {
+    T* const* src = UF == UF_PREDICT_OUT ? md.st[a.base_slot] : md.td[a.tprev];
+#pragma unroll
+    for (int k = 0; k < RPT; ++k)
+#pragma unroll
+      for (int f = 0; f < 3; ++f) pre[k][f] = (cval && r0 + k < w.rows) ? src[f][ob + k * N] : T(0);
+  }
+  tile_derive(md, t, false, given);
+  T* dst[3] = {nullptr, nullptr, nullptr};
+  T* tdst[3] = {nullptr, nullptr, nullptr};
+#pragma unroll
+  for (int f = 0; f < 3; ++f) {
+    if (UF == UF_PREDICT_IN || UF == UF_PREDICT_OUT) dst[f] = md.st[a.out_slot][f];
+    if (UF == UF_PREDICT_OUT || UF == UF_CORRECT) tdst[f] = md.td[a.tout][f];
+  }
+  const T h = em.h;
+#pragma unroll
+  for (int k = 0; k < RPT; ++k) {
+    const int r = r0 + k;
+    if (!cval || r >= w.rows) continue;
+    const int j = w.j0 + r, o = ob + k * N;
+    const int p = TL::pos(r + 1, c + 1);
+    const TileView<T, TL> sv{t, p, j};
+    const T du = point_du<T, PASS, ADV>(sv, ub_lon, ub_lat);
+    const T dv = point_dv<T, PASS, ADV>(sv, ub_lon, ub_lat);
+    const T dg = point_dgd<T, PASS>(sv);
+    if (UF == UF_PREDICT_IN) {
+      // update_state from the input level (src/dycore_mod.F90:609-633)
+      dst[F_IU][o] = t.iu[p] + h * du;
+      dst[F_IV][o] = t.iv[p] + h * dv;
+      dst[F_GD][o] = t.gd[p] + h * dg;
+    } else if (UF == UF_PREDICT_OUT) {
+      tdst[F_IU][o] = du;
+      dst[F_IU][o] = pre[k][F_IU] + h * du;
+      tdst[F_IV][o] = dv;
+      dst[F_IV][o] = pre[k][F_IV] + h * dv;
+      tdst[F_GD][o] = dg;
+      dst[F_GD][o] = pre[k][F_GD] + h * dg;
+    } else if (UF == UF_CORRECT) {
+      // inner_product_tend_tend (src/types_mod.F90:347-372), same order
+      // of terms as Emit::put
+      const T wf = t.cf(TF_COS, j), wh = t.ch(TH_COS, j);
+      tdst[F_IU][o] = du;
+      em.ip1.add(pre[k][F_IU] * du * wf);
+      em.ip2.add(du * du * wf);
+      tdst[F_IV][o] = dv;
+      em.ip1.add(pre[k][F_IV] * dv * wh);
+      em.ip2.add(dv * dv * wh);
+      tdst[F_GD][o] = dg;
+      em.ip1.add(pre[k][F_GD] * dg * wf);
+      em.ip2.add(dg * dg * wf);
+    } else {
+      em.put(F_IU, o, du, t.cf(TF_COS, j), em.base_of(F_IU, o), em.prev_of(F_IU, o));
+      em.put(F_IV, o, dv, t.ch(TH_COS, j), em.base_of(F_IV, o), em.prev_of(F_IV, o));
+      em.put(F_GD, o, dg, t.cf(TF_COS, j), em.base_of(F_GD, o), em.prev_of(F_GD, o));
+    }
+  }
+}
+
+// ------------------------------------------------------------ warp strips
+// One warp advances one strip: output columns i0..i0+cols-1 (cols <= 30) of
+// rows j0..j0+rows-1, all ordinary.  Lane L holds column i0-1+L (mod N) of
+// every field for the rows j-1, j, j+1 around the output row j in
+// registers; east and west neighbours come by shuffles, so the strip needs
+// no shared memory and no block barrier.  Lanes 1..cols emit.
+
+template <typename T, bool GIVEN>
+struct StripRaw;  // one row of one column as loaded (off the sphere: 0)
+template <typename T>
+struct StripRaw<T, false> {
+  T gd, ghs, iu, iv, gdx, ig;  // gdx: gd one column east (lane 31 only)
+};
+template <typename T>
+struct StripRaw<T, true> {
+  T gd, ghs, iu, iv, gdx, ig, gu, gv;  // gu, gv: the level's given u, v
+};
+template <typename T>
+struct StripRow {  // a row with its derived iap gd, u and v
+  T gd, ghs, iu, iv, ig, u, v;
+};
+
+// Coefficients come by shuffles: lanes 0..15 hold the record of row j,
+// lanes 16..31 that of row j+1; the one row j-1 coefficient the operators
+// read (half-row cos) is carried from the previous row.  Every lane must
+// evaluate the operators (shuffles need the whole warp).
+template <typename T>
+struct StripView {
+  int j;
+  T rec;       // this lane's coefficient record word
+  T cos_prev;  // ch(TH_COS, j - 1)
+  T u_[3][3], v_[3][3], iu_[3][3], iv_[3][3], ig_[3][3], gd_[3][3], ghs_[3][3];
+  __device__ __forceinline__ T u(int dr, int dc) const { return u_[dr + 1][dc + 1]; }
+  __device__ __forceinline__ T v(int dr, int dc) const { return v_[dr + 1][dc + 1]; }
+  __device__ __forceinline__ T iu(int dr, int dc) const { return iu_[dr + 1][dc + 1]; }
+  __device__ __forceinline__ T iv(int dr, int dc) const { return iv_[dr + 1][dc + 1]; }
+  __device__ __forceinline__ T ig(int dr, int dc) const { return ig_[dr + 1][dc + 1]; }
+  __device__ __forceinline__ T gd(int dr, int dc) const { return gd_[dr + 1][dc + 1]; }
+  __device__ __forceinline__ T ghs(int dr, int dc) const { return ghs_[dr + 1][dc + 1]; }
+  __device__ __forceinline__ T cf(int k, int jj) const { return coef(k, jj); }
+  __device__ __forceinline__ T ch(int k, int jj) const { return coef(k, jj); }
+  __device__ __forceinline__ T coef(int k, int jj) const {
+    if (jj == j - 1) return cos_prev;  // k == TH_COS
+    return __shfl_sync(0xffffffffu, rec, (jj == j ? 0 : kRecWords) + k);
+  }
+};
+
+template <typename T>
+__device__ __forceinline__ T shfl_dn(T x) {
+  return __shfl_down_sync(0xffffffffu, x, 1);
+}
+template <typename T>
+__device__ __forceinline__ T shfl_up(T x) {
+  return __shfl_up_sync(0xffffffffu, x, 1);
+}
+
+// Per-warp constants of a strip.
+template <typename T>
+struct StripCtx {
+  int c, cx, N, M, Mh;
+  bool east;
+  const T* __restrict__ gd;
+  const T* __restrict__ ghs;
+  const T* __restrict__ iu;
+  const T* __restrict__ iv;
+  const T* __restrict__ gu;
+  const T* __restrict__ gv;
+};
+
+template <typename T, bool GIVEN>
+__device__ __forceinline__ StripRaw<T, GIVEN> strip_load(const StripCtx<T>& x, int r) {
+  StripRaw<T, GIVEN> q;
+  const bool vf = r >= 0 && r < x.M, vh = r >= 0 && r < x.Mh;
+  const int o = r * x.N + x.c;
+  q.gd = vf ? x.gd[o] : T(0);
+  q.ghs = vf ? x.ghs[o] : T(0);
+  q.iu = vf ? x.iu[o] : T(0);
+  q.iv = vh ? x.iv[o] : T(0);
+  q.gdx = (vf && x.east) ? x.gd[r * x.N + x.cx] : T(0);
+  q.ig = T(0);
+  if constexpr (GIVEN) {
+    q.gu = vf ? x.gu[o] : T(0);
+    q.gv = vh ? x.gv[o] : T(0);
+  }
+  return q;
+}
+
+// Derive row r (raw a, iap gd already set) given the iap gd of row r+1.
+template <typename T, bool GIVEN>
+__device__ __forceinline__ StripRow<T> strip_derive(const StripCtx<T>& x, const StripRaw<T, GIVEN>& a, T ig_next,
+                                                    int r) {
+  StripRow<T> d;
+  d.gd = a.gd;
+  d.ghs = a.ghs;
+  d.iu = a.iu;
+  d.iv = a.iv;
+  d.ig = a.ig;
+  if constexpr (GIVEN) {
+    d.u = a.gu;
+    d.v = a.gv;
+  } else {
+    const T ige = shfl_dn(a.ig);  // iap gd one column east
+    const T ig_e = x.east ? sqrt(a.gdx) : ige;
+    d.u = (r >= 1 && r <= x.M - 2) ? a.iu * T(2) / (a.ig + ig_e) : T(0);
+    d.v = (r >= 0 && r < x.Mh) ? a.iv * T(2) / (a.ig + ig_next) : T(0);
+  }
+  return d;
+}
+
+template <typename T, int PASS, int ADV, int UF, bool GIVEN>
+__device__ void strip_warp(const MemberDev<T>& md, const WorkItem& w, const StageArgs& a) {
+  using Raw = StripRaw<T, GIVEN>;
+  const int lane = threadIdx.x & 31;
+  StripCtx<T> x;
+  x.N = md.N;
+  x.M = md.M;
+  x.Mh = md.Mh;
+  const int N = x.N;
+  x.c = ((w.i0 - 1 + lane) % N + N) % N;
+  x.cx = x.c + 1 < N ? x.c + 1 : 0;
+  x.east = lane == 31;
+  x.gd = md.st[a.in_slot][F_GD];
+  x.iu = md.st[a.in_slot][F_IU];
+  x.iv = md.st[a.in_slot][F_IV];
+  x.ghs = md.ghs;
+  x.gu = md.given_u;
+  x.gv = md.given_v;
+  const int c = x.c;
+  const bool emit = lane >= 1 && lane <= w.cols;
+  Emit<T> em(md, a, T(md.pcdt[PASS] * a.h_scale));
+  const T ub_lon = T(a.ub_lon), ub_lat = T(a.ub_lat);
+  const T h = em.h;
+  T* dst[3] = {nullptr, nullptr, nullptr};
+  T* tdst[3] = {nullptr, nullptr, nullptr};
+  const T* src[3] = {nullptr, nullptr, nullptr};
+#pragma unroll
+  for (int f = 0; f < 3; ++f) {
+    if (UF == UF_PREDICT_IN || UF == UF_PREDICT_OUT) dst[f] = md.st[a.out_slot][f];
+    if (UF == UF_PREDICT_OUT || UF == UF_CORRECT) tdst[f] = md.td[a.tout][f];
+    if (UF == UF_PREDICT_OUT) src[f] = md.st[a.base_slot][f];
+    if (UF == UF_CORRECT) src[f] = md.td[a.tprev][f];
+  }
+  // Member fields the loop reads, in registers: the stores below could
+  // otherwise alias the descriptor and force reloads.
+  const T* __restrict__ rc = md.rowc;
+  const int j0 = w.j0, jend = w.j0 + w.rows;  // output rows j0..jend-1
+  // Window: rows j0-1, j0, j0+1 derived; raw rows j0+2, j0+3 in hand (the
+  // loads of a row are issued two iterations before its derivation).
+  Raw r0 = strip_load<T, GIVEN>(x, j0 - 1);
+  Raw r1 = strip_load<T, GIVEN>(x, j0);
+  Raw r2 = strip_load<T, GIVEN>(x, j0 + 1);
+  Raw p1 = strip_load<T, GIVEN>(x, j0 + 2);
+  Raw p2 = strip_load<T, GIVEN>(x, j0 + 3);
+  T pre[3] = {T(0), T(0), T(0)};
+  if (UF == UF_PREDICT_OUT || UF == UF_CORRECT) {
+#pragma unroll
+    for (int f = 0; f < 3; ++f) pre[f] = emit ? src[f][j0 * N + c] : T(0);
+  }
+  r0.ig = sqrt(r0.gd);
+  r1.ig = sqrt(r1.gd);
+  r2.ig = sqrt(r2.gd);
+  p1.ig = sqrt(p1.gd);
+  StripRow<T> d0 = strip_derive<T, GIVEN>(x, r0, r1.ig, j0 - 1);
+  StripRow<T> d1 = strip_derive<T, GIVEN>(x, r1, r2.ig, j0);
+  StripRow<T> d2 = strip_derive<T, GIVEN>(x, r2, p1.ig, j0 + 1);
+  T d0_v_e = shfl_dn(d0.v), d0_iv_e = shfl_dn(d0.iv);  // row j-1, one column east
+  T d1_u_w = shfl_up(d1.u), d1_iu_w = shfl_up(d1.iu);  // row j, one column west
+  // Coefficient records of rows j, j+1 (one word per lane), of j+1, j+2
+  // for the next row, and the half-row cos of row j-1.
+  static_assert(2 * kRecWords == 32, "two records per warp");
+  T rec = __ldg(rc + (j0 + 1) * kRecWords + lane);
+  T cos_prev = __ldg(rc + j0 * kRecWords + TH_COS);
+  for (int j = j0; j < jend; ++j) {
+    // Loads for later rows: raw row j+4, update operands of row j+1.
+    Raw q;
+    if (j + 4 <= jend + 1)
+      q = strip_load<T, GIVEN>(x, j + 4);
+    else
+      q = Raw{};
+    const T rec_next = j + 1 < jend ? __ldg(rc + (j + 2) * kRecWords + lane) : T(0);
+    T pre_next[3] = {T(0), T(0), T(0)};
+    if (UF == UF_PREDICT_OUT || UF == UF_CORRECT) {
+      if (j + 1 < jend && emit) {
+#pragma unroll
+        for (int f = 0; f < 3; ++f) pre_next[f] = src[f][(j + 1) * N + c];
+      }
+    }
+    StripView<T> s;
+    s.j = j;
+    s.rec = rec;
+    s.cos_prev = cos_prev;
+    // row j-1
+    s.v_[0][1] = d0.v;
+    s.v_[0][2] = d0_v_e;
+    s.iu_[0][1] = d0.iu;
+    s.iv_[0][1] = d0.iv;
+    s.iv_[0][2] = d0_iv_e;
+    s.ig_[0][1] = d0.ig;
+    // row j
+    s.u_[1][0] = d1_u_w;
+    s.u_[1][1] = d1.u;
+    s.u_[1][2] = shfl_dn(d1.u);
+    s.v_[1][1] = d1.v;
+    s.v_[1][2] = shfl_dn(d1.v);
+    s.iu_[1][0] = d1_iu_w;
+    s.iu_[1][1] = d1.iu;
+    s.iu_[1][2] = shfl_dn(d1.iu);
+    s.iv_[1][0] = shfl_up(d1.iv);
+    s.iv_[1][1] = d1.iv;
+    s.iv_[1][2] = shfl_dn(d1.iv);
+    s.ig_[1][0] = shfl_up(d1.ig);
+    s.ig_[1][1] = d1.ig;
+    s.ig_[1][2] = shfl_dn(d1.ig);
+    s.gd_[1][1] = d1.gd;
+    s.gd_[1][2] = shfl_dn(d1.gd);
+    s.ghs_[1][1] = d1.ghs;
+    s.ghs_[1][2] = shfl_dn(d1.ghs);
+    // row j+1
+    const T d2_u_w = shfl_up(d2.u), d2_iu_w = shfl_up(d2.iu);
+    s.u_[2][0] = d2_u_w;
+    s.u_[2][1] = d2.u;
+    s.v_[2][1] = d2.v;
+    s.iu_[2][0] = d2_iu_w;
+    s.iu_[2][1] = d2.iu;
+    s.iv_[2][1] = d2.iv;
+    s.ig_[2][1] = d2.ig;
+    s.gd_[2][1] = d2.gd;
+    s.ghs_[2][1] = d2.ghs;
+    const T du = point_du<T, PASS, ADV>(s, ub_lon, ub_lat);
+    const T dv = point_dv<T, PASS, ADV>(s, ub_lon, ub_lat);
+    const T dg = point_dgd<T, PASS>(s);
+    const T wf = s.cf(TF_COS, j), wh = s.ch(TH_COS, j);
+    if (emit) {
+      const int o = j * N + c;
+      if (UF == UF_PREDICT_IN) {
+        dst[F_IU][o] = d1.iu + h * du;
+        dst[F_IV][o] = d1.iv + h * dv;
+        dst[F_GD][o] = d1.gd + h * dg;
+      } else if (UF == UF_PREDICT_OUT) {
+        tdst[F_IU][o] = du;
+        dst[F_IU][o] = pre[F_IU] + h * du;
+        tdst[F_IV][o] = dv;
+        dst[F_IV][o] = pre[F_IV] + h * dv;
+        tdst[F_GD][o] = dg;
+        dst[F_GD][o] = pre[F_GD] + h * dg;
+      } else if (UF == UF_CORRECT) {
+        tdst[F_IU][o] = du;
+        em.ip1.add(pre[F_IU] * du * wf);
+        em.ip2.add(du * du * wf);
+        tdst[F_IV][o] = dv;
+        em.ip1.add(pre[F_IV] * dv * wh);
+        em.ip2.add(dv * dv * wh);
+        tdst[F_GD][o] = dg;
+        em.ip1.add(pre[F_GD] * dg * wf);
+        em.ip2.add(dg * dg * wf);
+      } else {
+        em.put(F_IU, o, du, wf, em.base_of(F_IU, o), em.prev_of(F_IU, o));
+        em.put(F_IV, o, dv, wh, em.base_of(F_IV, o), em.prev_of(F_IV, o));
+        em.put(F_GD, o, dg, wf, em.base_of(F_GD, o), em.prev_of(F_GD, o));
+      }
+    }
+    cos_prev = wh;
+    rec = rec_next;
+    // Advance the window by one row: derive row j+2 (raw p1, with the iap
+    // gd of row j+3 from p2).
+    p2.ig = sqrt(p2.gd);
+    const StripRow<T> d3 = strip_derive<T, GIVEN>(x, p1, p2.ig, j + 2);
+    d0_v_e = s.v_[1][2];
+    d0_iv_e = s.iv_[1][2];
+    d1_u_w = d2_u_w;
+    d1_iu_w = d2_iu_w;
+    d0 = d1;
+    d1 = d2;
+    d2 = d3;
+    p1 = p2;
+    p2 = q;
+#pragma unroll
+    for (int f = 0; f < 3; ++f) pre[f] = pre_next[f];
+  }
+  if (a.do_ip) {
+    warp_acc(em.ip1);
+    warp_acc(em.ip2);
+    if (lane == 0) {
+      double* pp = a.partials + 4 * (size_t)w.pidx;
+      pp[0] = (double)em.ip1.s;
+      pp[1] = (double)em.ip1.c;
+      pp[2] = (double)em.ip2.s;
+      pp[3] = (double)em.ip2.c;
+    }
+  }
+}
+
+template <typename T, int PASS, int ADV, int UF>
+__device__ __forceinline__ void strip_item(const MemberDev<T>& md, const WorkItem& w, const StageArgs& a) {
+  // u, v supplied with this level (initial condition, diffusion): used as
+  // given, as the reference's space_operators reads state%u / state%v.
+  const bool given = a.uvslot && a.uvslot[w.member] == a.in_slot;
+  if (a.uvslot && a.out_slot >= 0 && (threadIdx.x & 31) == 0 && a.uvslot[w.member] == a.out_slot)
+    a.uvslot[w.member] = -1;  // level overwritten: u, v derived from now on
+  if (given)
+    strip_warp<T, PASS, ADV, UF, true>(md, w, a);
+  else
+    strip_warp<T, PASS, ADV, UF, false>(md, w, a);
+}
+
+// The end of a whole-row task once the row's raw tendencies are in shared
+// memory (rdu, rdv, rdg; N each): the pole cap of dgd (from the FP64 sum
+// `cap` of this block), the zonal filters, and the update.
+template <typename T, int PASS>
+__device__ void row_tail(const MemberDev<T>& md, const StageArgs& a, Emit<T>& em, int j, T* rdu, T* rdv, T* rdg,
+                         const Acc<double>& cap, T* coefs, T* redT, const T* gd_in, const T* iu_in,
+                         const T* iv_in, const T* tw) {
+  const int N = md.N, M = md.M, Mh = md.Mh;
+  const int info = md.rowinfo[j];
+  const bool has_du = (j >= 1 && j <= M - 2);
+  const bool has_dv = (j <= Mh - 1);
+  const bool south = (j == 0), north = (j == M - 1);
+  if ((south || north) && PASS != kSlowPass) {
+    double* redD = reinterpret_cast<double*>(redT + 64);
+    double s = block_value(cap, redD);
+    if (north) s = -s;
+    s = s * 2.0 / N / kRadius / (kPi / Mh);
+    // dgd = - mass_div_lon - mass_div_lat with mass_div_lon = 0 at poles
+    const T val = T(-0.0) - T(s);
+    for (int i = threadIdx.x; i < N; i += blockDim.x) rdg[i] = val;
+    __syncthreads();
+  }
+  const size_t ro = (size_t)j * N;
+  if (has_du && (info & RI_FLAG_FULL))
+    filter_rescale(md, rdu, iu_in + ro, (const T*)nullptr, ri_keep_full(info), coefs, redT, a.rescale_rtol, tw);
+  if (has_dv && (info & RI_FLAG_HALF))
+    filter_rescale(md, rdv, iv_in + ro, (const T*)nullptr, ri_keep_half(info), coefs, redT, a.rescale_rtol, tw);
+  if (PASS != kSlowPass && (info & RI_FLAG_FULL))
+    filter_rescale(md, rdg, gd_in + ro, md.ghs + ro, ri_keep_full(info), coefs, redT, a.rescale_rtol, tw);
+  const T cj = cf(md, CF_COS, j);
+  const T chj = has_dv ? ch(md, CH_COS, j) : T(0);
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const size_t o = ro + i;
+    // du is 0 on pole rows (never assigned by the reference); inner
+    // products skip pole-row du (src/types_mod.F90:355).
+    if (has_du)
+      em.put(F_IU, o, rdu[i], cj, em.base_of(F_IU, o), em.prev_of(F_IU, o));
+    else
+      em.put(F_IU, o, T(0), T(0), em.base_of(F_IU, o), T(0));
+    if (has_dv) em.put(F_IV, o, rdv[i], chj, em.base_of(F_IV, o), em.prev_of(F_IV, o));
+    em.put(F_GD, o, rdg[i], cj, em.base_of(F_GD, o), em.prev_of(F_GD, o));
+  }
+}
+
 template <typename T>
 struct StageOcc {
   static constexpr int kMinBlocks = sizeof(T) == 4 ? 4 : 2;
@@ -569,7 +1033,8 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
   T* staging = reinterpret_cast<T*>(smem_raw);
   T* rows = staging + staging_words;  // 3 * max_n (row tasks)
   T* coefs = rows + 3 * max_n;        // kMaxKeep
-  T* redT = coefs + kMaxKeep;         // 64
+  T* redT = coefs + kMaxKeep;         // 64, then 64 doubles
+  T* tw = redT + 64 + 64 * (int)(sizeof(double) / sizeof(T));  // 2 * max_n twiddles
   __shared__ MemberDev<T> smd;
 
   const WorkItem w = wl[blockIdx.x];
@@ -582,7 +1047,6 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
   const double hstep = md.pcdt[PASS] * a.h_scale;
   Emit<T> em(md, a, T(hstep));
   const T ub_lon = T(a.ub_lon), ub_lat = T(a.ub_lat);
-  const bool plain_ops = a.taccum < 0 && a.tadd < 0 && a.tadd2 < 0;
   // u, v supplied with this level (initial condition, diffusion): used as
   // given, as the reference's space_operators reads state%u / state%v.
   const bool given = a.uvslot && a.uvslot[w.member] == a.in_slot;
@@ -591,61 +1055,24 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
 
   if (w.kind == 0) {
     // ---------------- bulk tile: rows j0..j0+R-1 are ordinary rows
-    using TL = Tile<T, R, W>;
-    constexpr int PPT = (R * W + kThreads - 1) / kThreads;
-    TL t = carve<T, R, W>(staging, w.j0, w.i0, w.rows, w.cols);
-    tile_issue(md, gd_in, iu_in, iv_in, t, given);
-    // While the tile is in flight, fetch the per-point update operands.
-    const bool base_in_tile = a.out_slot >= 0 && a.base_slot == a.in_slot;
-    T pre_b[PPT][3], pre_p[PPT][3];
-#pragma unroll
-    for (int k = 0; k < PPT; ++k) {
-      const int q = threadIdx.x + k * kThreads;
-#pragma unroll
-      for (int f = 0; f < 3; ++f) {
-        pre_b[k][f] = T(0);
-        pre_p[k][f] = T(0);
-      }
-      const int r = q / W, c = q - r * W;
-      if (q < R * W && r < w.rows && c < w.cols) {
-        const size_t o = (size_t)(w.j0 + r) * N + (w.i0 + c);
-#pragma unroll
-        for (int f = 0; f < 3; ++f) {
-          if (a.out_slot >= 0 && !base_in_tile) pre_b[k][f] = md.st[a.base_slot][f][o];
-          if (a.do_ip) pre_p[k][f] = a.beta_mode == 0 ? md.td[a.tprev][f][o] : md.st[a.ip_slot][f][o];
-        }
-      }
+#define GDC_BULK(F)                                                                                   \
+  bulk_tile<T, PASS, ADV, R, W, F>(md, a, w, staging, given, gd_in, iu_in, iv_in, ub_lon, ub_lat, em); \
+  break;
+    switch (a.form) {
+      case UF_PREDICT_IN:
+        GDC_BULK(UF_PREDICT_IN)
+      case UF_PREDICT_OUT:
+        GDC_BULK(UF_PREDICT_OUT)
+      case UF_CORRECT:
+        GDC_BULK(UF_CORRECT)
+      default:
+        GDC_BULK(UF_GENERAL)
     }
-    tile_derive(md, t, false, given);
-#pragma unroll
-    for (int k = 0; k < PPT; ++k) {
-      const int q = threadIdx.x + k * kThreads;
-      const int r = q / W, c = q - r * W;
-      if (q >= R * W || r >= w.rows || c >= w.cols) continue;
-      const int j = w.j0 + r, i = w.i0 + c;
-      const int p = TL::pos(r + 1, c + 1);
-      const size_t o = (size_t)j * N + i;
-      if (base_in_tile) {
-        pre_b[k][F_GD] = t.gd[p];
-        pre_b[k][F_IU] = t.iu[p];
-        pre_b[k][F_IV] = t.iv[p];
-      }
-      const T du = point_du<T, PASS, ADV>(md, t, j, p, ub_lon, ub_lat);
-      const T dv = point_dv<T, PASS, ADV>(md, t, j, p, ub_lon, ub_lat);
-      const T dg = point_dgd<T, PASS>(md, t, j, p);
-      if (plain_ops) {
-        em.put(F_IU, o, du, t.cf(TF_COS, j), pre_b[k][F_IU], pre_p[k][F_IU]);
-        em.put(F_IV, o, dv, t.ch(TH_COS, j), pre_b[k][F_IV], pre_p[k][F_IV]);
-        em.put(F_GD, o, dg, t.cf(TF_COS, j), pre_b[k][F_GD], pre_p[k][F_GD]);
-      } else {
-        em.put(F_IU, o, du, t.cf(TF_COS, j), em.base_of(F_IU, o), em.prev_of(F_IU, o));
-        em.put(F_IV, o, dv, t.ch(TH_COS, j), em.base_of(F_IV, o), em.prev_of(F_IV, o));
-        em.put(F_GD, o, dg, t.cf(TF_COS, j), em.base_of(F_GD, o), em.prev_of(F_GD, o));
-      }
-    }
+#undef GDC_BULK
   } else {
     // ---------------- whole-row task: row index j (full row j, half row j)
     const int j = w.j0;
+    twiddles_to_shared(md, tw);
     const int info = md.rowinfo[j];
     const bool has_du = (j >= 1 && j <= M - 2);
     const bool has_dv = (j <= Mh - 1);
@@ -664,8 +1091,9 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
       for (int c = threadIdx.x; c < vw; c += blockDim.x) {
         const int p = TR::pos(1, c + 1);
         const int i = c0 + c;
-        rdu[i] = has_du ? point_du<T, PASS, ADV>(md, t, j, p, ub_lon, ub_lat) : T(0);
-        rdv[i] = has_dv ? point_dv<T, PASS, ADV>(md, t, j, p, ub_lon, ub_lat) : T(0);
+        const TileView<T, TR> sv{t, p, j};
+        rdu[i] = has_du ? point_du<T, PASS, ADV>(sv, ub_lon, ub_lat) : T(0);
+        rdv[i] = has_dv ? point_dv<T, PASS, ADV>(sv, ub_lon, ub_lat) : T(0);
         if (south || north) {
           // src/dycore_mod.F90:572-596: sp += (ig(j)+ig(j+1)) iv(j);
           // np -= (ig(j)+ig(j-1)) iv(j-1).  Terms and sum in FP64.
@@ -677,41 +1105,12 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
           }
           rdg[i] = T(0);
         } else {
-          rdg[i] = point_dgd<T, PASS>(md, t, j, p);
+          rdg[i] = point_dgd<T, PASS>(sv);
         }
       }
     }
     __syncthreads();
-    if ((south || north) && PASS != kSlowPass) {
-      double* redD = reinterpret_cast<double*>(redT + 64);
-      double s = block_value(cap, redD);
-      if (north) s = -s;
-      s = s * 2.0 / N / kRadius / (kPi / Mh);
-      // dgd = - mass_div_lon - mass_div_lat with mass_div_lon = 0 at poles
-      const T val = T(-0.0) - T(s);
-      for (int i = threadIdx.x; i < N; i += blockDim.x) rdg[i] = val;
-      __syncthreads();
-    }
-    const size_t ro = (size_t)j * N;
-    if (has_du && (info & RI_FLAG_FULL))
-      filter_rescale(md, rdu, iu_in + ro, (const T*)nullptr, ri_keep_full(info), coefs, redT, a.rescale_rtol);
-    if (has_dv && (info & RI_FLAG_HALF))
-      filter_rescale(md, rdv, iv_in + ro, (const T*)nullptr, ri_keep_half(info), coefs, redT, a.rescale_rtol);
-    if (PASS != kSlowPass && (info & RI_FLAG_FULL))
-      filter_rescale(md, rdg, gd_in + ro, md.ghs + ro, ri_keep_full(info), coefs, redT, a.rescale_rtol);
-    const T cj = cf(md, CF_COS, j);
-    const T chj = has_dv ? ch(md, CH_COS, j) : T(0);
-    for (int i = threadIdx.x; i < N; i += blockDim.x) {
-      const size_t o = ro + i;
-      // du is 0 on pole rows (never assigned by the reference); inner
-      // products skip pole-row du (src/types_mod.F90:355).
-      if (has_du)
-        em.put(F_IU, o, rdu[i], cj, em.base_of(F_IU, o), em.prev_of(F_IU, o));
-      else
-        em.put(F_IU, o, T(0), T(0), em.base_of(F_IU, o), T(0));
-      if (has_dv) em.put(F_IV, o, rdv[i], chj, em.base_of(F_IV, o), em.prev_of(F_IV, o));
-      em.put(F_GD, o, rdg[i], cj, em.base_of(F_GD, o), em.prev_of(F_GD, o));
-    }
+    row_tail<T, PASS>(md, a, em, j, rdu, rdv, rdg, cap, coefs, redT, gd_in, iu_in, iv_in, tw);
   }
 
   if (a.do_ip) {
@@ -727,6 +1126,34 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
       pp[2] = (double)s2.s;
       pp[3] = (double)s2.c;
     }
+  }
+}
+
+// Warp strips, one per warp (items cover every row of their members).
+template <typename T>
+struct StripOcc {
+  static constexpr int kMinBlocks = sizeof(T) == 4 ? GDC_STRIP_BLOCKS : 2;
+};
+
+template <typename T, int PASS, int ADV>
+__global__ void __launch_bounds__(kThreads, StripOcc<T>::kMinBlocks)
+    strip_kernel(const MemberDev<T>* __restrict__ mems, const WorkItem* __restrict__ wl, int nitems, StageArgs a) {
+  const int item = (int)blockIdx.x * (kThreads / 32) + (int)(threadIdx.x >> 5);
+  if (item >= nitems) return;
+  const WorkItem w = wl[item];
+  const MemberDev<T>& md = mems[w.member];
+  switch (a.form) {
+    case UF_PREDICT_IN:
+      strip_item<T, PASS, ADV, UF_PREDICT_IN>(md, w, a);
+      break;
+    case UF_PREDICT_OUT:
+      strip_item<T, PASS, ADV, UF_PREDICT_OUT>(md, w, a);
+      break;
+    case UF_CORRECT:
+      strip_item<T, PASS, ADV, UF_CORRECT>(md, w, a);
+      break;
+    default:
+      strip_item<T, PASS, ADV, UF_GENERAL>(md, w, a);
   }
 }
 
@@ -760,50 +1187,85 @@ __global__ void __launch_bounds__(kThreads)
 // levels carry a compensation word: new = (hi + lo) + dt*T via TwoSum.
 
 template <typename T>
-__device__ inline void final_point(const MemberDev<T>& md, const FinalArgs& a, int f, size_t o, double hstep) {
-  const T tv = md.td[a.tslot][f][o];
-  const T hi = md.st[a.base_slot][f][o];
-  if (a.use_lo) {
-    const T lo = md.lo[a.base_slot][f][o];
-    const T y = lo + T(hstep) * tv;
-    const T s = hi + y;
-    const T bp = s - hi;
-    const T err = (hi - (s - bp)) + (y - bp);
-    md.st[a.out_slot][f][o] = s;
-    md.lo[a.out_slot][f][o] = err;
-  } else {
-    md.st[a.out_slot][f][o] = hi + T(hstep) * tv;
-  }
-}
+struct Vec16;
+template <>
+struct Vec16<float> {
+  using type = float4;
+};
+template <>
+struct Vec16<double> {
+  using type = double2;
+};
 
+// One flat item: a contiguous run of one field, 16 bytes per access.  All
+// of a thread's loads are issued before its first store.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-    final_kernel(const MemberDev<T>* __restrict__ mems, const WorkItem* __restrict__ wl, FinalArgs a) {
-  __shared__ MemberDev<T> smd;
-  const WorkItem w = wl[blockIdx.x];
-  load_member(mems, w.member, &smd);
-  const MemberDev<T>& md = smd;
-  const int N = md.N, Mh = md.Mh;
+    final_kernel(const MemberDev<T>* __restrict__ mems, const FlatItem* __restrict__ fl, FinalArgs a) {
+  using V = typename Vec16<T>::type;
+  constexpr int VEC = 16 / (int)sizeof(T), U = flat_chunk<T>() / (VEC * kThreads);
+  const FlatItem w = fl[blockIdx.x];
+  const MemberDev<T>& md = mems[w.member];
   double hstep = md.pcdt[a.pass] * a.h_scale;
   if (a.beta) hstep = md.pcdt[a.pass] * a.h_scale * a.beta[w.member];
   // This level's u, v are derived from its new state from now on.
-  if (a.uvslot && threadIdx.x == 0 && a.uvslot[w.member] == a.out_slot) a.uvslot[w.member] = -1;
-  if (w.kind == 0) {
-    const int npts = w.rows * w.cols;
-    for (int q = threadIdx.x; q < npts; q += blockDim.x) {
-      const int r = q / w.cols, c = q - r * w.cols;
-      const size_t o = (size_t)(w.j0 + r) * N + (w.i0 + c);
-      final_point(md, a, F_GD, o, hstep);
-      final_point(md, a, F_IU, o, hstep);
-      final_point(md, a, F_IV, o, hstep);
+  if (a.uvslot && threadIdx.x == 0 && w.field == 0 && w.begin == 0 && a.uvslot[w.member] == a.out_slot)
+    a.uvslot[w.member] = -1;
+  const int f = w.field, nv = w.count / VEC;
+  const T h = T(hstep);
+  const V* __restrict__ tv = reinterpret_cast<const V*>(md.td[a.tslot][f] + w.begin);
+  const V* __restrict__ hi = reinterpret_cast<const V*>(md.st[a.base_slot][f] + w.begin);
+  V* __restrict__ out = reinterpret_cast<V*>(md.st[a.out_slot][f] + w.begin);
+  V x[U], t[U], l[U];
+#pragma unroll
+  for (int k = 0; k < U; ++k) {
+    const int q = threadIdx.x + k * kThreads;
+    if (q < nv) {
+      x[k] = hi[q];
+      t[k] = tv[q];
+    }
+  }
+  if (a.use_lo) {
+    const V* __restrict__ lo = reinterpret_cast<const V*>(md.lo[a.base_slot][f] + w.begin);
+    V* __restrict__ olo = reinterpret_cast<V*>(md.lo[a.out_slot][f] + w.begin);
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+      const int q = threadIdx.x + k * kThreads;
+      if (q < nv) l[k] = lo[q];
+    }
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+      const int q = threadIdx.x + k * kThreads;
+      if (q >= nv) continue;
+      V sv, ev;
+      const T* xs = reinterpret_cast<const T*>(&x[k]);
+      const T* ls = reinterpret_cast<const T*>(&l[k]);
+      const T* ts = reinterpret_cast<const T*>(&t[k]);
+      T* ss = reinterpret_cast<T*>(&sv);
+      T* es = reinterpret_cast<T*>(&ev);
+#pragma unroll
+      for (int m = 0; m < VEC; ++m) {
+        const T y = ls[m] + h * ts[m];
+        const T sum = xs[m] + y;
+        const T bp = sum - xs[m];
+        ss[m] = sum;
+        es[m] = (xs[m] - (sum - bp)) + (y - bp);
+      }
+      out[q] = sv;
+      olo[q] = ev;
     }
   } else {
-    const int j = w.j0;
-    for (int i = threadIdx.x; i < N; i += blockDim.x) {
-      const size_t o = (size_t)j * N + i;
-      final_point(md, a, F_GD, o, hstep);
-      final_point(md, a, F_IU, o, hstep);
-      if (j <= Mh - 1) final_point(md, a, F_IV, o, hstep);
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+      const int q = threadIdx.x + k * kThreads;
+      if (q >= nv) continue;
+      V sv;
+      const T* xs = reinterpret_cast<const T*>(&x[k]);
+      const T* ts = reinterpret_cast<const T*>(&t[k]);
+      T* ss = reinterpret_cast<T*>(&sv);
+#pragma unroll
+      for (int m = 0; m < VEC; ++m) ss[m] = xs[m] + h * ts[m];
+      out[q] = sv;
     }
   }
 }
@@ -811,53 +1273,114 @@ __global__ void __launch_bounds__(kThreads)
 // ------------------------------------------------------------- diag
 // diag_run totals (src/diag_mod.F90:301-317, 98-121) in FP64.
 
-template <typename T>
-__device__ inline double val64(const MemberDev<T>& md, int slot, int f, size_t o) {
-  double v = (double)md.st[slot][f][o];
-  if (md.lo[slot][f]) v += (double)md.lo[slot][f][o];
-  return v;
-}
+// One row j of the diag sums, by one warp.  FP64 members add the weighted
+// point terms in double-double (as the oracle's exact sums); FP32 members
+// sum each row's unweighted terms in float-float (the state is hi + lo) and
+// apply the row's FP64 weights once per row.
+struct FF {
+  float hi = 0.f, lo = 0.f;
+  __device__ void add(float x) {
+    const float t = hi + x;
+    const float bp = t - hi;
+    lo += (hi - (t - bp)) + (x - bp);
+    hi = t;
+  }
+  __device__ void add_sq(float xh, float xl) {  // (xh + xl)^2, dropping xl^2
+    const float p = xh * xh;
+    float e = fmaf(xh, xh, -p);
+    e = fmaf(2.0f * xh, xl, e);
+    add(p);
+    lo += e;
+  }
+  __device__ double value() const { return (double)hi + (double)lo; }
+};
 
-template <typename T>
-__global__ void __launch_bounds__(kThreads)
-    diag_kernel(const MemberDev<T>* __restrict__ mems, const WorkItem* __restrict__ wl, DiagArgs a) {
-  __shared__ double red[64];
-  __shared__ MemberDev<T> smd;
-  const WorkItem w = wl[blockIdx.x];
-  load_member(mems, w.member, &smd);
-  const MemberDev<T>& md = smd;
+__device__ inline void diag_row(const MemberDev<double>& md, int slot, int j, int lane, Acc<double>& mass,
+                                Acc<double>& en) {
   const int N = md.N, M = md.M, Mh = md.Mh;
   const double* dc = md.dcoef;
-  typename DiagAcc<T>::type mass, en;
-  auto point = [&](int j, int i, bool hv) {
-    const size_t o = (size_t)j * N + i;
-    const double g = val64(md, a.slot, F_GD, o);
-    const double gh = (double)md.ghs[o];
-    mass.add(dc[j] * g);
-    if (j >= 1 && j <= M - 2) {
-      const double uu = val64(md, a.slot, F_IU, o);
-      en.add(uu * uu * dc[M + j]);
+  const bool hu = j >= 1 && j <= M - 2, hv = j < Mh;
+  const size_t ro = (size_t)j * N;
+  const double2* g2 = reinterpret_cast<const double2*>(md.st[slot][F_GD] + ro);
+  const double2* h2 = reinterpret_cast<const double2*>(md.ghs + ro);
+  const double2* u2 = reinterpret_cast<const double2*>(md.st[slot][F_IU] + ro);
+  const double2* v2 = reinterpret_cast<const double2*>(md.st[slot][F_IV] + (hv ? ro : 0));
+  const double wm = dc[j], wf = dc[M + j], wh = hv ? dc[2 * M + j] : 0.0;
+  for (int q = lane; q < N / 2; q += 32) {
+    const double2 g = g2[q], gh = h2[q];
+    const double2 uu = hu ? u2[q] : make_double2(0, 0);
+    const double2 vv = hv ? v2[q] : make_double2(0, 0);
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const double gk = k ? g.y : g.x, hk = k ? gh.y : gh.x;
+      const double uk = k ? uu.y : uu.x, vk = k ? vv.y : vv.x;
+      mass.add(wm * gk);
+      if (hu) en.add(uk * uk * wf);
+      if (hv) en.add(vk * vk * wh);
+      const double hh = gk + hk;
+      en.add(hh * hh * wf);
     }
-    if (hv) {
-      const double vv = val64(md, a.slot, F_IV, o);
-      en.add(vv * vv * dc[2 * M + j]);
-    }
-    const double hh = g + gh;
-    en.add(hh * hh * dc[M + j]);
-  };
-  if (w.kind == 0) {
-    const int npts = w.rows * w.cols;
-    for (int q = threadIdx.x; q < npts; q += blockDim.x) {
-      const int r = q / w.cols, c = q - r * w.cols;
-      point(w.j0 + r, w.i0 + c, true);
-    }
-  } else {
-    for (int i = threadIdx.x; i < N; i += blockDim.x) point(w.j0, i, w.j0 <= Mh - 1);
   }
+}
+
+__device__ inline void diag_row(const MemberDev<float>& md, int slot, int j, int lane, PlainD& mass, PlainD& en) {
+  const int N = md.N, M = md.M, Mh = md.Mh;
+  const double* dc = md.dcoef;
+  const bool hu = j >= 1 && j <= M - 2, hv = j < Mh;
+  const size_t ro = (size_t)j * N;
+  const float4* gH = reinterpret_cast<const float4*>(md.st[slot][F_GD] + ro);
+  const float4* gL = reinterpret_cast<const float4*>(md.lo[slot][F_GD] + ro);
+  const float4* hS = reinterpret_cast<const float4*>(md.ghs + ro);
+  const float4* uH = reinterpret_cast<const float4*>(md.st[slot][F_IU] + ro);
+  const float4* uL = reinterpret_cast<const float4*>(md.lo[slot][F_IU] + ro);
+  const float4* vH = reinterpret_cast<const float4*>(md.st[slot][F_IV] + (hv ? ro : 0));
+  const float4* vL = reinterpret_cast<const float4*>(md.lo[slot][F_IV] + (hv ? ro : 0));
+  FF sg, su, sv, sh;
+  const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int q = lane; q < N / 4; q += 32) {
+    const float4 gh = gH[q], gl = gL[q], hs = hS[q];
+    const float4 uh = hu ? uH[q] : z, ul = hu ? uL[q] : z;
+    const float4 vh = hv ? vH[q] : z, vl = hv ? vL[q] : z;
+    const float* a0 = &gh.x;
+    const float* a1 = &gl.x;
+    const float* a2 = &hs.x;
+    const float* a3 = &uh.x;
+    const float* a4 = &ul.x;
+    const float* a5 = &vh.x;
+    const float* a6 = &vl.x;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      sg.add(a0[k]);
+      sg.lo += a1[k];
+      su.add_sq(a3[k], a4[k]);
+      sv.add_sq(a5[k], a6[k]);
+      // hh = g + ghs as a float pair
+      const float t = a0[k] + a2[k];
+      const float bp = t - a0[k];
+      const float e = (a0[k] - (t - bp)) + (a2[k] - bp) + a1[k];
+      sh.add_sq(t, e);
+    }
+  }
+  mass.add(dc[j] * sg.value());
+  if (hu) en.add(dc[M + j] * su.value());
+  if (hv) en.add(dc[2 * M + j] * sv.value());
+  en.add(dc[M + j] * sh.value());
+}
+
+// Warp w of item (member, rows begin..begin+count-1) sums row begin + w.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    diag_kernel(const MemberDev<T>* __restrict__ mems, const FlatItem* __restrict__ dl, DiagArgs a) {
+  __shared__ double red[64];
+  const FlatItem w = dl[blockIdx.x];
+  const MemberDev<T>& md = mems[w.member];
+  typename DiagAcc<T>::type mass, en;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp < w.count) diag_row(md, a.slot, w.begin + warp, lane, mass, en);
   const auto sm = block_acc(mass, red);
   const auto se = block_acc(en, red);
   if (threadIdx.x == 0) {
-    double* pp = a.partials + 4 * (size_t)w.pidx;
+    double* pp = a.partials + 4 * (size_t)blockIdx.x;
     pp[0] = sm.s;
     pp[1] = sm.c;
     pp[2] = se.s;
@@ -872,8 +1395,8 @@ __global__ void __launch_bounds__(kThreads)
   const int s = slots[blockIdx.x];
   const MemberDev<T>& md = mems[s];
   Acc<double> m, e;
-  for (int q = threadIdx.x; q < md.pcount; q += blockDim.x) {
-    const double* pp = a.partials + 4 * (size_t)(md.pbase + q);
+  for (int q = threadIdx.x; q < md.dcount; q += blockDim.x) {
+    const double* pp = a.partials + 4 * (size_t)(md.dbase + q);
     m.merge(pp[0], pp[1]);
     e.merge(pp[2], pp[3]);
   }
@@ -941,12 +1464,14 @@ __global__ void __launch_bounds__(kThreads)
   T* coefs = rows + 3 * max_n;
   T* redT = coefs + kMaxKeep;
   double* redD = reinterpret_cast<double*>(redT + 64);
+  T* tw = redT + 64 + 64 * (int)(sizeof(double) / sizeof(T));  // 2 * max_n twiddles
   __shared__ MemberDev<T> smd;
   const WorkItem w = wl[blockIdx.x];
   load_member(mems, w.member, &smd);
   const MemberDev<T>& md = smd;
   const int N = md.N, M = md.M, Mh = md.Mh;
   const T* gd_in = md.st[slot][F_GD];
+  if (w.kind != 0) twiddles_to_shared(md, tw);
   T* go = md.st[SL_SA][F_GD];
   T* uo = md.st[SL_SA][F_IU];
   T* vo = md.st[SL_SA][F_IV];
@@ -1018,10 +1543,10 @@ __global__ void __launch_bounds__(kThreads)
       __syncthreads();
     }
     if (has_u && (info & RI_FLAG_FULL)) {
-      filter_project(md, rg, ri_keep_full(info), coefs);
-      filter_project(md, ru, ri_keep_full(info), coefs);
+      filter_project(md, rg, ri_keep_full(info), coefs, tw);
+      filter_project(md, ru, ri_keep_full(info), coefs, tw);
     }
-    if (has_v && (info & RI_FLAG_HALF)) filter_project(md, rv, ri_keep_half(info), coefs);
+    if (has_v && (info & RI_FLAG_HALF)) filter_project(md, rv, ri_keep_half(info), coefs, tw);
     __syncthreads();
     for (int i = threadIdx.x; i < N; i += blockDim.x) {
       const size_t o = (size_t)j * N + i;
@@ -1125,7 +1650,8 @@ size_t stage_smem_bytes(int tile_rows, int tile_cols, int max_n, int* staging_wo
   const int sw = ((bulk > row ? bulk : row) + 3) & ~3;
   max_n = (max_n + 1) & ~1;
   if (staging_words) *staging_words = sw;
-  return (size_t)(sw + 3 * max_n + kMaxKeep + 64) * sizeof(T) + 64 * sizeof(double) + 16;
+  return (size_t)(sw + 3 * max_n + kMaxKeep + 64) * sizeof(T) + 64 * sizeof(double) + 2 * (size_t)max_n * sizeof(T) +
+         16;
 }
 
 template <typename T, int PASS, int ADV, int R, int W>
@@ -1162,12 +1688,41 @@ static int launch_stage_shape(const MemberDev<T>* mem, const WorkItem* wl, int n
 
 template <typename T>
 int launch_stage(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int adv, int tile_rows, int tile_cols,
-                 int max_n, const StageArgs& a, void* stream) {
+                 int max_n, const StageArgs& args, void* stream) {
   if (nwork <= 0) return GDC_OK;
   cudaStream_t s = (cudaStream_t)stream;
+  StageArgs a = args;
+  a.form = update_form(args);
   if (tile_rows == 8 && tile_cols == 32) return launch_stage_shape<T, 8, 32>(mem, wl, nwork, adv, max_n, a, s);
   if (tile_rows == 8 && tile_cols == 64) return launch_stage_shape<T, 8, 64>(mem, wl, nwork, adv, max_n, a, s);
   if (tile_rows == 4 && tile_cols == 128) return launch_stage_shape<T, 4, 128>(mem, wl, nwork, adv, max_n, a, s);
+  return GDC_E_CONFIG;
+}
+
+template <typename T, int PASS, int ADV>
+static int launch_strips_t(const WorkItem* strips, int nstrip, const MemberDev<T>* mem, const StageArgs& a,
+                           cudaStream_t s) {
+  if (nstrip <= 0) return GDC_OK;
+  const int per = kThreads / 32;
+  strip_kernel<T, PASS, ADV><<<(nstrip + per - 1) / per, kThreads, 0, s>>>(mem, strips, nstrip, a);
+  return check_launch();
+}
+
+template <typename T>
+int launch_stage_strips(const MemberDev<T>* mem, const WorkItem* strips, int nstrip, int adv, const StageArgs& args,
+                        void* stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  StageArgs a = args;
+  a.form = update_form(args);
+#define GDC_DISPATCH(P, A) \
+  if (a.pass == P && adv == A) return launch_strips_t<T, P, A>(strips, nstrip, mem, a, s);
+  GDC_DISPATCH(kAllPass, GDC_ADV_CENTER_DIFF)
+  GDC_DISPATCH(kFastPass, GDC_ADV_CENTER_DIFF)
+  GDC_DISPATCH(kSlowPass, GDC_ADV_CENTER_DIFF)
+  GDC_DISPATCH(kAllPass, GDC_ADV_UPWIND)
+  GDC_DISPATCH(kFastPass, GDC_ADV_UPWIND)
+  GDC_DISPATCH(kSlowPass, GDC_ADV_UPWIND)
+#undef GDC_DISPATCH
   return GDC_E_CONFIG;
 }
 
@@ -1180,17 +1735,17 @@ int launch_beta(const MemberDev<T>* mem, const int* slots, int nmembers, const d
 }
 
 template <typename T>
-int launch_final(const MemberDev<T>* mem, const WorkItem* wl, int nwork, const FinalArgs& a, void* stream) {
-  if (nwork <= 0) return GDC_OK;
-  final_kernel<T><<<nwork, kThreads, 0, (cudaStream_t)stream>>>(mem, wl, a);
+int launch_final(const MemberDev<T>* mem, const FlatItem* fl, int nflat, const FinalArgs& a, void* stream) {
+  if (nflat <= 0) return GDC_OK;
+  final_kernel<T><<<nflat, kThreads, 0, (cudaStream_t)stream>>>(mem, fl, a);
   return check_launch();
 }
 
 template <typename T>
-int launch_diag(const MemberDev<T>* mem, const WorkItem* wl, int nwork, const int* slots, int nmembers,
+int launch_diag(const MemberDev<T>* mem, const FlatItem* dl, int ndl, const int* slots, int nmembers,
                 const DiagArgs& a, void* stream) {
-  if (nwork <= 0) return GDC_OK;
-  diag_kernel<T><<<nwork, kThreads, 0, (cudaStream_t)stream>>>(mem, wl, a);
+  if (ndl <= 0) return GDC_OK;
+  diag_kernel<T><<<ndl, kThreads, 0, (cudaStream_t)stream>>>(mem, dl, a);
   int rc = check_launch();
   if (rc) return rc;
   diag_finalize_kernel<T><<<nmembers, kThreads, 0, (cudaStream_t)stream>>>(mem, slots, a);

@@ -9,8 +9,9 @@ template int launch_diffusion<float>(const MemberDev<float>*, const WorkItem*, i
 template int launch_copy_state<float>(const MemberDev<float>*, const WorkItem*, int, int, int, void*);
 template int launch_stage<float>(const MemberDev<float>*, const WorkItem*, int, int, int, int, int,
                                  const StageArgs&, void*);
-template int launch_final<float>(const MemberDev<float>*, const WorkItem*, int, const FinalArgs&, void*);
-template int launch_diag<float>(const MemberDev<float>*, const WorkItem*, int, const int*, int, const DiagArgs&, void*);
+template int launch_stage_strips<float>(const MemberDev<float>*, const WorkItem*, int, int, const StageArgs&, void*);
+template int launch_final<float>(const MemberDev<float>*, const FlatItem*, int, const FinalArgs&, void*);
+template int launch_diag<float>(const MemberDev<float>*, const FlatItem*, int, const int*, int, const DiagArgs&, void*);
 template int launch_beta<float>(const MemberDev<float>*, const int*, int, const double*, double*, int, int, void*);
 
 }  // namespace gdc

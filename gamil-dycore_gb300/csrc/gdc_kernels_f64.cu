@@ -12,8 +12,9 @@ template int launch_diffusion<double>(const MemberDev<double>*, const WorkItem*,
 template int launch_copy_state<double>(const MemberDev<double>*, const WorkItem*, int, int, int, void*);
 template int launch_stage<double>(const MemberDev<double>*, const WorkItem*, int, int, int, int, int,
                                   const StageArgs&, void*);
-template int launch_final<double>(const MemberDev<double>*, const WorkItem*, int, const FinalArgs&, void*);
-template int launch_diag<double>(const MemberDev<double>*, const WorkItem*, int, const int*, int, const DiagArgs&, void*);
+template int launch_stage_strips<double>(const MemberDev<double>*, const WorkItem*, int, int, const StageArgs&, void*);
+template int launch_final<double>(const MemberDev<double>*, const FlatItem*, int, const FinalArgs&, void*);
+template int launch_diag<double>(const MemberDev<double>*, const FlatItem*, int, const int*, int, const DiagArgs&, void*);
 template int launch_beta<double>(const MemberDev<double>*, const int*, int, const double*, double*, int, int, void*);
 
 }  // namespace gdc

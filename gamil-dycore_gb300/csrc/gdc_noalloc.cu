@@ -113,6 +113,7 @@ extern "C" int gdc_tendency_noalloc(const gdc_params* p, int pass, const double*
     coef[ch_off(CH_DLON, M) + j + 1] = co.half_dlon[j];
     coef[ch_off(CH_DLAT, M) + j + 1] = co.half_dlat[j];
   }
+  const std::vector<double> rowc = row_records(coef, M);
   std::vector<double> twid(2 * (size_t)N);
   for (int k = 0; k < N; ++k) {
     twid[k] = std::cos(2.0 * kPi * k / N);
@@ -154,6 +155,8 @@ extern "C" int gdc_tendency_noalloc(const gdc_params* p, int pass, const double*
   off = up256(off + wl.size() * sizeof(WorkItem));
   const size_t o_coef = off;
   off = up256(off + coef.size() * sizeof(double));
+  const size_t o_rowc = off;
+  off = up256(off + rowc.size() * sizeof(double));
   const size_t o_twid = off;
   off = up256(off + twid.size() * sizeof(double));
   const size_t o_row = off;
@@ -178,6 +181,7 @@ extern "C" int gdc_tendency_noalloc(const gdc_params* p, int pass, const double*
   d.td[TS_NEW][F_IV] = dv;
   d.ghs = const_cast<double*>(ghs);
   d.coef = reinterpret_cast<const double*>(base + o_coef);
+  d.rowc = reinterpret_cast<const double*>(base + o_rowc);
   d.twid = reinterpret_cast<const double*>(base + o_twid);
   d.rowinfo = reinterpret_cast<const int*>(base + o_row);
   d.given_u = const_cast<double*>(given_u);
@@ -194,6 +198,8 @@ extern "C" int gdc_tendency_noalloc(const gdc_params* p, int pass, const double*
     e = cudaMemcpyAsync(base + o_wl, wl.data(), wl.size() * sizeof(WorkItem), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(base + o_coef, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(base + o_rowc, rowc.data(), rowc.size() * sizeof(double), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(base + o_twid, twid.data(), twid.size() * sizeof(double), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess)
