@@ -261,6 +261,20 @@ def plain_fp64(gdc, torch, ts, steps=360):
             "l2_fp32_vs_fp64": {"gd": rl2(s32[2], s64[2]), "u": rl2(s32[0], s64[0]), "v": rl2(s32[1], s64[1])}}
 
 
+def serve_sample(gdc, ts, n=40, rate=20.0, seed=0):
+    """The serving loop on the first `n` requests of the Poisson stream
+    (20 requests/s; grids 180x91..1440x721; 6 h to 5 days), FP32."""
+    from gdc import serve
+    reqs = serve.poisson_stream(n=2000, rate=rate, seed=seed)[:n]
+    srv = serve.Server(precision=gdc.FP32, steps_per_tick=4, cuda_stream=ts.cuda_stream)
+    st = srv.run(reqs)
+    srv.close()
+    st.update({"max_resident": srv.max_resident, "ticks": srv.ticks, "steps_per_tick": 4,
+               "sample": f"first {n} of 2000 requests of the Poisson stream (rate {rate}/s, seed {seed}); "
+                         f"offered load exceeds one GPU's rate, so latency includes queueing"})
+    return st
+
+
 def cpu_baseline_sample(seconds_target=12.0):
     """The oracle (port of the reference, 1 thread) on a 360x181 member."""
     import gdc
@@ -310,6 +324,7 @@ def run_ours(args, rank, world, dist):
     e2e_ms, e2e_gpt, h2d, d2h = e2e_batch(gdc, torch, members, args.steps, gdc.FP32)
     e2e_ms = reduce_max(dist, e2e_ms)
     prof_ms, prof_n = profile_kernels(gdc, members, gdc.FP32)
+    serving = serve_sample(gdc, ts) if rank == 0 else None
     if rank != 0:
         return
     # Roofline of the dominant kernel (the fused stage kernel): algorithmic
@@ -322,7 +337,7 @@ def run_ours(args, rank, world, dist):
     hbm = pk.get("hbm_gbs")
     peak_src = "measured" if hbm else "fallback"
     hbm = hbm or 6800.0
-    algo_bytes = 312 * 4  # 39 words x (6 + 2) predict_correct calls per grid-point-step
+    algo_bytes = gdc.algorithmic_bytes_per_gpt_step(scheme(gdc, gdc.FP32))
     line = {
         "metric": "grid-pt-steps/s batched FP32 vs plain FP64 on GB300 @L2<=1e-5; p50/p99 latency",
         "value": value,
@@ -356,6 +371,7 @@ def run_ours(args, rank, world, dist):
                        "fp32_single_member_value": plain["fp32_value"],
                        "l2_fp32_vs_fp64_after_1_day": plain["l2_fp32_vs_fp64"],
                        "batched_fp32_over_plain_fp64": value / plain["value"]},
+        "serving": serving,
         "nan_members": sum(1 for x in nan if x >= 0),
         "cpu_baseline": cpu_baseline_sample(),
     }

@@ -1368,20 +1368,25 @@ int gdc_batch_profile(gdc_batch* b, int nsteps, double* ms, long long* launches)
 
 double gdc_algorithmic_bytes_per_gpt_step(const gdc_params* p) {
   if (!p) return 0;
-  // Prognostic words {gd, iap u, iap v} (+ ghs) read and written per
-  // predict_correct call: stage 1 reads 4 writes 3, stage 2 reads 7 writes
-  // 6, stage 3 reads 7 writes 3, the final update reads 6 writes 3: 39.
+  // Words of {gd, iap u, iap v} (+ ghs) read and written per grid point by
+  // one predict_correct call: stage 1 reads 4 writes 3, stage 2 reads 7
+  // writes 6, stage 3 reads 7 writes 3, the final update reads 6 writes 3:
+  // 39.  FP32 time levels carry a compensation word per field, which the
+  // final update reads and writes too (+6).  The diagnostics read the new
+  // level and ghs once per step (4 words, 7 with compensation words).
+  const bool fp32 = p->precision == GDC_FP32;
+  const double pc = 39.0 + (fp32 ? 6.0 : 0.0);
   double calls = 1;
   if (p->split_scheme == GDC_SPLIT_CSP2) calls = p->subcycles + 2;
-  double words = 39.0 * calls;
+  double words = pc * calls;
   if (p->split_scheme == GDC_SPLIT_ISP) {
     // copy 6, slow tendency 7, per subcycle 13 + 13 + 16, slow 13 + 13 + 13,
-    // final update 9.
-    words = 6 + 7 + p->subcycles * 42.0 + 39 + 9;
+    // final update 9 (+6 compensation words).
+    words = 6 + 7 + p->subcycles * 42.0 + 39 + 9 + (fp32 ? 6.0 : 0.0);
   }
   if (p->use_diffusion) words += 6;
-  const double wbytes = p->precision == GDC_FP32 ? 4.0 : 8.0;
-  return words * wbytes;
+  words += fp32 ? 7.0 : 4.0;
+  return words * (fp32 ? 4.0 : 8.0);
 }
 
 // ---- single model

@@ -1,0 +1,198 @@
+"""Forecast serving with continuous batching on one GPU.
+
+Requests (a grid, a forecast length and an arrival time) are admitted into
+one ``gdc.Batch`` as they arrive and as free device memory allows
+(``gdc_batch_add`` refuses a member that would leave less than
+``reserve_bytes`` free); their state stays resident on the device and every
+tick advances all resident members together in the batched step.  A member
+that reaches its length is read back (optionally), removed, and its memory
+serves the next request.  Time to completion is measured from arrival.
+
+The reference has no serving path: this loop is built on the batch engine's
+C ABI (``gdc_batch_add / _step / _sync / _member_info / _remove``), and the
+engine's per-member arithmetic does not depend on the other members, so a
+request's result is the same alone and in the mix.
+"""
+from __future__ import annotations
+
+import collections
+import dataclasses
+import math
+import time
+
+import numpy as np
+
+from . import E_OOM, FP32, G, SPLIT_CSP2, Batch, GdcError, default_params, ic_add_noise, ic_seeded
+
+# grid (degrees of resolution) -> num_lon, num_lat, time step (240 s per
+# degree), steps per model day, filter cutoffs of the near-pole rows
+GRIDS = {
+    180: (180, 91, 480.0, 180, [4] * 3),
+    360: (360, 181, 240.0, 360, [4] * 5),
+    720: (720, 361, 120.0, 720, [4] * 10),
+    1440: (1440, 721, 60.0, 1440, [4] * 20),
+}
+
+
+@dataclasses.dataclass
+class Request:
+    rid: int
+    grid: int            # key of GRIDS
+    nsteps: int
+    arrival: float       # seconds after the start of the stream
+    admitted: float = math.nan
+    finished: float = math.nan
+    member: int = -1
+    nan_step: int = -1
+    result: tuple | None = None
+
+    @property
+    def points(self) -> int:
+        N, M = GRIDS[self.grid][:2]
+        return N * M
+
+    @property
+    def latency(self) -> float:
+        return self.finished - self.arrival
+
+
+def poisson_stream(n: int = 2000, rate: float = 20.0, seed: int = 0, grids=(180, 360, 720, 1440),
+                   min_hours: float = 6.0, max_days: float = 5.0) -> list[Request]:
+    """The request stream: Poisson arrivals at `rate` per second, grid drawn
+    uniformly from `grids`, forecast length uniform in [min_hours, max_days]."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, size=n))
+    g = rng.choice(np.asarray(grids), size=n)
+    length_s = rng.uniform(min_hours * 3600.0, max_days * 86400.0, size=n)
+    out = []
+    for k in range(n):
+        dt = GRIDS[int(g[k])][2]
+        out.append(Request(rid=k, grid=int(g[k]), nsteps=max(1, int(round(length_s[k] / dt))), arrival=float(t[k])))
+    return out
+
+
+def serving_scheme(precision: int = FP32):
+    """csp2 with 8 fast subcycles: the batch shares one subcycle count, and
+    at 1440x721 (dt 60 s, 20 filtered rows per pole) 6 subcycles exceed the
+    fast-wave CFL limit next to the filtered rows (the seeded state goes NaN
+    after about 1.3 model days); 8 keep it stable."""
+    return default_params(num_lon=360, num_lat=181, time_step_size=240.0, subcycles=8, split_scheme=SPLIT_CSP2,
+                          qcon_modified=1, use_zonal_tend_filter=1, zonal_tend_filter_cutoff_wavenumber=[4] * 5,
+                          precision=precision)
+
+
+class InitialStates:
+    """Seeded initial states: the degree 1..6 harmonic state of each grid
+    (built once per grid) plus N(0, 1 m) noise on gd seeded per request."""
+
+    def __init__(self, seed: int = 0, noise_m: float = 1.0):
+        self.seed = seed
+        self.noise = noise_m * G
+        self.base = {}
+
+    def __call__(self, req: Request):
+        N, M = GRIDS[req.grid][:2]
+        if req.grid not in self.base:
+            self.base[req.grid] = ic_seeded(N, M, seed=self.seed)
+        u, v, gd, ghs = self.base[req.grid]
+        gd = ic_add_noise(gd.copy(), N, M, seed=1000 + req.rid, sigma=self.noise)
+        return u, v, gd, ghs
+
+
+class Server:
+    """The request loop.  `batch_factory` builds the engine (a ``gdc.Batch``
+    by default); `steps_per_tick` model steps are taken between admission and
+    completion checks."""
+
+    def __init__(self, precision: int = FP32, steps_per_tick: int = 4, reserve_bytes: int = 2 << 30,
+                 max_members: int = 1000, batch_factory=None, initial_states=None, clock=time.perf_counter,
+                 sleep=time.sleep, cuda_stream: int | None = None):
+        self.steps_per_tick = steps_per_tick
+        self.reserve = reserve_bytes
+        self.max_members = max_members
+        self.clock = clock
+        self.sleep = sleep
+        self.ics = initial_states or InitialStates()
+        self.batch = batch_factory() if batch_factory else Batch(serving_scheme(precision))
+        if cuda_stream is not None:
+            self.batch.set_stream(cuda_stream)
+        self.ticks = 0
+        self.max_resident = 0
+
+    def close(self):
+        self.batch.close()
+
+    def run(self, requests: list[Request], keep_results: bool = False, max_wall: float | None = None) -> dict:
+        """Serve `requests` (sorted by arrival).  With `max_wall`, arrivals
+        after that many seconds are not admitted and the loop ends once the
+        admitted requests complete."""
+        reqs = sorted(requests, key=lambda r: r.arrival)
+        waiting = collections.deque()
+        running: dict[int, Request] = {}
+        done: list[Request] = []
+        nxt = 0
+        t0 = self.clock()
+        while True:
+            now = self.clock() - t0
+            cutoff = now if max_wall is None else min(now, max_wall)
+            while nxt < len(reqs) and reqs[nxt].arrival <= cutoff:
+                waiting.append(reqs[nxt])
+                nxt += 1
+            # admission: first come first served, while memory and slots last
+            while waiting and len(running) < self.max_members:
+                r = waiting[0]
+                N, M, dt, _, cut = GRIDS[r.grid]
+                try:
+                    mid = self.batch.add(N, M, dt, r.nsteps, *self.ics(r), reserve_bytes=self.reserve, cutoff=cut)
+                except GdcError as e:
+                    if e.code == E_OOM and running:
+                        break  # wait for completions to free memory
+                    raise
+                r.member = mid
+                r.admitted = self.clock() - t0
+                running[mid] = r
+                waiting.popleft()
+            self.max_resident = max(self.max_resident, len(running))
+            arrivals_left = nxt < len(reqs) and (max_wall is None or reqs[nxt].arrival <= max_wall)
+            if not running:
+                if not arrivals_left and not waiting:
+                    break
+                if arrivals_left:
+                    self.sleep(max(0.0, reqs[nxt].arrival - (self.clock() - t0)))
+                continue
+            self.batch.step(self.steps_per_tick)
+            self.batch.sync()
+            self.ticks += 1
+            now = self.clock() - t0
+            for mid, r in list(running.items()):
+                steps, fin, nan = self.batch.info(mid)
+                if fin or nan >= 0:
+                    r.finished = now
+                    r.nan_step = nan
+                    if keep_results:
+                        r.result = self.batch.get_state(mid)
+                    self.batch.remove(mid)
+                    del running[mid]
+                    done.append(r)
+        return summarize(done, len(reqs))
+
+
+def summarize(done: list[Request], offered: int) -> dict:
+    if not done:
+        return {"completed": 0, "offered": offered}
+    lat = np.array([r.latency for r in done])
+    wait = np.array([r.admitted - r.arrival for r in done])
+    work = sum(r.points * r.nsteps for r in done)
+    span = max(r.finished for r in done) - min(r.arrival for r in done)
+    return {
+        "completed": len(done),
+        "offered": offered,
+        "p50_s": float(np.percentile(lat, 50)),
+        "p99_s": float(np.percentile(lat, 99)),
+        "mean_s": float(lat.mean()),
+        "p50_admission_wait_s": float(np.percentile(wait, 50)),
+        "gpt_steps": float(work),
+        "span_s": float(span),
+        "gpt_steps_per_s": float(work / span) if span > 0 else float("nan"),
+        "nan_members": int(sum(1 for r in done if r.nan_step >= 0)),
+    }

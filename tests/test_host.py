@@ -82,7 +82,9 @@ def test_reference_ic_hooks(native):
 
 def test_algorithmic_bytes(native):
     p = gdc.default_params(split_scheme=gdc.SPLIT_CSP2, subcycles=6, precision=gdc.FP32)
-    assert gdc.algorithmic_bytes_per_gpt_step(p) == 39 * 8 * 4
+    # 8 predict_correct calls of 39 words (+6 compensation words in FP32)
+    # and the diagnostics' read of the new level (7 words FP32, 4 FP64)
+    assert gdc.algorithmic_bytes_per_gpt_step(p) == (45 * 8 + 7) * 4
     p.precision = gdc.FP64
-    assert gdc.algorithmic_bytes_per_gpt_step(p) == 39 * 8 * 8
+    assert gdc.algorithmic_bytes_per_gpt_step(p) == (39 * 8 + 4) * 8
     assert gdc.member_bytes(p, 360, 181) > 20 * 360 * 181 * 8

@@ -1,0 +1,125 @@
+"""Serving loop: the request stream and the scheduling logic, on the CPU
+against a fake batch engine (no device calls)."""
+import numpy as np
+import pytest
+
+import gdc
+from gdc import serve
+
+
+def test_poisson_stream_matches_the_configuration():
+    reqs = serve.poisson_stream(n=2000, rate=20.0, seed=3)
+    t = np.array([r.arrival for r in reqs])
+    assert np.all(np.diff(t) > 0)
+    assert abs(np.mean(np.diff(t)) - 1 / 20.0) < 0.05 / 20.0 * 3
+    grids = [r.grid for r in reqs]
+    assert set(grids) == {180, 360, 720, 1440}
+    for g in (180, 360, 720, 1440):
+        assert abs(grids.count(g) / 2000 - 0.25) < 0.05
+    for r in reqs:
+        dt = serve.GRIDS[r.grid][2]
+        length = r.nsteps * dt
+        assert 6 * 3600 - dt <= length <= 5 * 86400 + dt
+    # the time step is 240 s per degree of resolution
+    assert [serve.GRIDS[g][2] for g in (180, 360, 720, 1440)] == [480.0, 240.0, 120.0, 60.0]
+    again = serve.poisson_stream(n=2000, rate=20.0, seed=3)
+    assert [(r.grid, r.nsteps, r.arrival) for r in again] == [(r.grid, r.nsteps, r.arrival) for r in reqs]
+
+
+class FakeClock:
+    def __init__(self):
+        self.t = 0.0
+
+    def __call__(self):
+        return self.t
+
+    def sleep(self, s):
+        self.t += max(s, 0.0)
+
+
+class FakeBatch:
+    """Members advance one step per step(); each step costs `step_s` of
+    fake time per resident member; admission fails past `capacity`."""
+
+    def __init__(self, clock, capacity=3, step_s=0.01):
+        self.clock, self.capacity, self.step_s = clock, capacity, step_s
+        self.members = {}
+        self.next_id = 0
+        self.adds = []
+
+    def add(self, N, M, dt, nsteps, u, v, gd, ghs, reserve_bytes=0, cutoff=None):
+        if len(self.members) >= self.capacity:
+            raise gdc.GdcError(gdc.E_OOM, "full")
+        mid = self.next_id
+        self.next_id += 1
+        self.members[mid] = [0, nsteps]
+        self.adds.append((mid, N, nsteps))
+        return mid
+
+    def step(self, n):
+        for _ in range(n):
+            self.clock.t += self.step_s * max(1, len(self.members))
+            for m in self.members.values():
+                if m[0] < m[1]:
+                    m[0] += 1
+
+    def sync(self):
+        pass
+
+    def info(self, mid):
+        s, n = self.members[mid]
+        return s, s >= n, -1
+
+    def get_state(self, mid):
+        return ("state", mid)
+
+    def remove(self, mid):
+        del self.members[mid]
+
+    def set_stream(self, s):
+        pass
+
+    def close(self):
+        pass
+
+
+def fake_server(capacity=3, steps_per_tick=2):
+    clock = FakeClock()
+    fb = FakeBatch(clock, capacity=capacity)
+    srv = serve.Server(steps_per_tick=steps_per_tick, batch_factory=lambda: fb, initial_states=lambda r: (0, 0, 0, 0),
+                       clock=clock, sleep=clock.sleep)
+    return srv, fb, clock
+
+
+def test_server_admits_by_memory_and_completes_everything():
+    reqs = [serve.Request(rid=k, grid=180, nsteps=3 + k, arrival=0.001 * k) for k in range(8)]
+    srv, fb, clock = fake_server(capacity=3)
+    stats = srv.run(reqs, keep_results=True)
+    assert stats["completed"] == 8 and stats["offered"] == 8
+    assert srv.max_resident == 3  # admission stopped at the memory limit
+    assert [a[0] for a in fb.adds] == list(range(8))  # first come, first served
+    for r in reqs:
+        assert r.arrival <= r.admitted <= r.finished
+        assert r.result == ("state", r.member)
+    lat = [r.latency for r in reqs]
+    assert stats["p50_s"] == pytest.approx(np.percentile(lat, 50))
+    assert stats["p99_s"] == pytest.approx(np.percentile(lat, 99))
+    assert stats["gpt_steps"] == sum(r.points * r.nsteps for r in reqs)
+    assert not fb.members  # every member removed
+
+
+def test_server_idles_until_the_next_arrival_and_honours_max_wall():
+    reqs = [serve.Request(rid=0, grid=360, nsteps=2, arrival=1.0),
+            serve.Request(rid=1, grid=360, nsteps=2, arrival=5.0),
+            serve.Request(rid=2, grid=360, nsteps=2, arrival=50.0)]
+    srv, fb, clock = fake_server(capacity=4)
+    stats = srv.run(reqs, max_wall=10.0)
+    assert stats["completed"] == 2 and stats["offered"] == 3
+    assert reqs[0].admitted >= 1.0 and reqs[1].admitted >= 5.0
+    assert np.isnan(reqs[2].finished)
+
+
+def test_server_raises_when_a_request_can_never_fit():
+    srv, fb, clock = fake_server(capacity=0)
+    with pytest.raises(gdc.GdcError):
+        srv.run([serve.Request(rid=0, grid=180, nsteps=1, arrival=0.0)])
