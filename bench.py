@@ -275,6 +275,50 @@ def serve_sample(gdc, ts, n=40, rate=20.0, seed=0):
     return st
 
 
+def large_run(args):
+    """1440x721, dt 60 s, FP32 (compensated levels; FP64 pole caps and
+    integrals) for args.days model days, and the FP64 path (bitwise equal to
+    the oracle) for args.fp64_days: mass and total-energy drift per day,
+    relative L2 of gd, u, v FP32 vs FP64 at the last FP64 day.  Initial
+    state: degree 1..12 seeded harmonics plus 3 seeded 2000 m mountains."""
+    import numpy as np
+    import __graft_entry__
+    __graft_entry__.build()
+    import gdc
+    N, M, dt, spd, cut = GRIDS[1440]
+    ic = gdc.ic_seeded(N, M, seed=0, lmax=12, n_mountains=3, mountain_height=2000.0, mountain_radius_deg=20.0)
+    out = {"workload": "large-run", "grid": f"{N}x{M}", "dt": dt, "subcycles": 8, "days": args.days,
+           "fp64_days": args.fp64_days}
+    states = {}
+    for prec, days in ((gdc.FP32, args.days), (gdc.FP64, args.fp64_days)):
+        p = gdc.default_params(num_lon=N, num_lat=M, time_step_size=dt, subcycles=8, split_scheme=gdc.SPLIT_CSP2,
+                               qcon_modified=1, zonal_tend_filter_cutoff_wavenumber=cut, precision=prec)
+        b = gdc.Batch(p)
+        mid = b.add(N, M, dt, days * spd, *ic)
+        m0, e0, _ = b.diag(mid)
+        rows = []
+        t = time.perf_counter()
+        for d in range(1, days + 1):
+            b.step(spd)
+            b.sync()
+            m, e, beta = b.diag(mid)
+            rows.append({"day": d, "mass_drift": (m - m0) / m0, "energy_drift": (e - e0) / e0, "beta": beta,
+                         "nan_step": b.info(mid)[2]})
+        secs = time.perf_counter() - t
+        states[prec] = b.get_state(mid)
+        b.close()
+        key = "fp32" if prec == gdc.FP32 else "fp64"
+        out[key] = {"per_day": rows, "seconds": secs, "grid_pt_steps_per_s": N * M * days * spd / secs}
+
+    def rl2(a, b):
+        x, y = a[2:-2, 2:-2], b[2:-2, 2:-2]
+        return float(np.sqrt(np.sum((x - y) ** 2) / np.sum(y * y)))
+    s32, s64 = states[gdc.FP32], states[gdc.FP64]
+    if args.days == args.fp64_days:
+        out["l2_fp32_vs_fp64"] = {"gd": rl2(s32[2], s64[2]), "u": rl2(s32[0], s64[0]), "v": rl2(s32[1], s64[1])}
+    print(json.dumps(out), flush=True)
+
+
 def cpu_baseline_sample(seconds_target=12.0):
     """The oracle (port of the reference, 1 thread) on a 360x181 member."""
     import gdc
@@ -445,7 +489,11 @@ def main():
     ap.add_argument("--steps", type=int, default=720)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="batch", choices=["batch"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "large-run"],
+                    help="large-run: 1440x721 FP32 for --days model days with per-day mass and energy drift, "
+                         "beside the FP64 path for --fp64-days")
+    ap.add_argument("--days", type=int, default=10)
+    ap.add_argument("--fp64-days", type=int, default=2)
     ap.add_argument("--profile-only", action="store_true",
                     help="run warmup+steps of the ensemble batch and exit (for ncu)")
     args = ap.parse_args()
@@ -455,6 +503,8 @@ def main():
         int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), None)
     if args.impl == "reference":
         run_reference(args, rank, world, dist)
+    elif args.workload == "large-run":
+        large_run(args)
     else:
         run_ours(args, rank, world, dist)
     if dist is not None:
