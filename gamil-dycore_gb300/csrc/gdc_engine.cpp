@@ -522,7 +522,8 @@ class Batch final : public BatchIface {
     const bool st = strip_shape_supported(r, c);
     if (!st && !tile_shape_supported(r, c))
       return fail(GDC_E_CONFIG,
-                  "set_tile: supported shapes are tiles 8x32, 8x64, 4x128 and warp strips 8x30, 16x30, 32x30, 64x30");
+                  "set_tile: supported shapes are tiles 8x32, 8x64, 4x128, 16x64 and warp strips "
+                  "8x30, 16x30, 32x30, 64x30");
     tile_r = r;
     tile_c = c;
     strips = st;
@@ -540,7 +541,7 @@ class Batch final : public BatchIface {
   // Times each candidate tile shape on the current members (graph replay,
   // CUDA events) and keeps the fastest.  Advances the members.
   int autotune(int* rr, int* cc, double* best_ms) override {
-    static const int cand[][2] = {{8, 32}, {8, 64}, {4, 128}, {16, 30}, {32, 30}};
+    static const int cand[][2] = {{8, 32}, {8, 64}, {16, 64}, {4, 128}, {16, 30}};
     double best = 1e30;
     int br = tile_r, bc = tile_c;
     for (auto& c : cand) {
@@ -711,12 +712,16 @@ class Batch final : public BatchIface {
   std::vector<Prof> prof;
   std::vector<void*> allocs;
 
-  // FP32: 8x64 tiles (fastest of the layouts on the 64-member ensemble);
-  // FP64 is arithmetic-bound: 8x32 tiles spread the rows over more SMs.
-  static int default_rows() { return 8; }
-  static int default_cols() { return sizeof(T) == 4 ? 64 : 32; }
+  // Fastest measured: FP32 16x64 tiles on the 64-member ensemble, FP64
+  // 8x64 on the single 360x181 member.
+  static int default_rows() { return sizeof(T) == 4 ? 16 : 8; }
+  static int default_cols() { return 64; }
 
-  const WorkItem* tile_list() const { return strips ? d_twl : d_wl; }
+  // The diffusion and copy kernels run on 8x32, 8x64 or 4x128 tiles.
+  bool own_tile_list() const {
+    return strips || !((tile_r == 8 && (tile_c == 32 || tile_c == 64)) || (tile_r == 4 && tile_c == 128));
+  }
+  const WorkItem* tile_list() const { return own_tile_list() ? d_twl : d_wl; }
 
   int fail(int code, const std::string& m) {
     err = m;
@@ -862,7 +867,7 @@ class Batch final : public BatchIface {
     nwork = (int)hwl.size();
     nrow = (int)rows_first.size();
     std::vector<WorkItem> htwl;
-    if (strips) {
+    if (own_tile_list()) {
       int pt = 0;
       std::vector<WorkItem> trows, ttiles;
       for (int s : active_slots) {
@@ -873,7 +878,7 @@ class Batch final : public BatchIface {
       htwl = trows;
       htwl.insert(htwl.end(), ttiles.begin(), ttiles.end());
     }
-    ntwork = strips ? (int)htwl.size() : nwork;
+    ntwork = own_tile_list() ? (int)htwl.size() : nwork;
     hflat.clear();
     for (int s : active_slots) {
       const int n[3] = {recs[s].N * recs[s].M, recs[s].N * recs[s].M, recs[s].N * (recs[s].M - 1)};
@@ -902,7 +907,7 @@ class Batch final : public BatchIface {
       cudaError_t e = cudaMalloc(&d_flat, flat_cap * sizeof(FlatItem));
       if (e != cudaSuccess) return fail(GDC_E_OOM, cuda_msg("rebuild: flat list", e));
     }
-    if (strips && (size_t)ntwork > twl_cap) {
+    if (own_tile_list() && (size_t)ntwork > twl_cap) {
       if (d_twl) cudaFree(d_twl);
       d_twl = nullptr;
       twl_cap = std::max<size_t>(ntwork, 2 * twl_cap);
@@ -925,7 +930,7 @@ class Batch final : public BatchIface {
     }
     cudaError_t e = cudaSuccess;
     if (nwork) e = cudaMemcpy(d_wl, hwl.data(), nwork * sizeof(WorkItem), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && strips && ntwork)
+    if (e == cudaSuccess && own_tile_list() && ntwork)
       e = cudaMemcpy(d_twl, htwl.data(), ntwork * sizeof(WorkItem), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && nflat)
       e = cudaMemcpy(d_flat, hflat.data(), nflat * sizeof(FlatItem), cudaMemcpyHostToDevice);
@@ -1137,7 +1142,8 @@ class Batch final : public BatchIface {
         cudaEventCreate(&e1);
         cudaEventRecord(e0, stream);
       }
-      rc = launch_diffusion<T>(d_mem, tile_list(), ntwork, strips ? 8 : tile_r, strips ? 32 : tile_c, max_n, new_, c,
+      rc = launch_diffusion<T>(d_mem, tile_list(), ntwork, own_tile_list() ? 8 : tile_r, own_tile_list() ? 32 : tile_c,
+                               max_n, new_, c,
                                d_uvslot, stream);
       if (pr) {
         cudaEventRecord(e1, stream);

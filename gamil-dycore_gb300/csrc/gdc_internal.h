@@ -232,7 +232,7 @@ struct DiagArgs {
 // Tile shapes compiled for the stage and diffusion kernels (rows x columns),
 // and the warp-strip layouts of the stage kernel (band rows x kStripCols).
 inline bool tile_shape_supported(int r, int c) {
-  return (r == 8 && c == 32) || (r == 8 && c == 64) || (r == 4 && c == 128);
+  return (r == 8 && c == 32) || (r == 8 && c == 64) || (r == 4 && c == 128) || (r == 16 && c == 64);
 }
 inline bool strip_shape_supported(int r, int c) { return c == kStripCols && (r == 8 || r == 16 || r == 32 || r == 64); }
 

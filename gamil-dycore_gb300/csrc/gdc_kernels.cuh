@@ -1643,6 +1643,7 @@ size_t stage_smem_bytes(int tile_rows, int tile_cols, int max_n, int* staging_wo
   int bulk = 0;
   if (tile_rows == 8 && tile_cols == 32) bulk = tile_words<T, 8, 32>();
   if (tile_rows == 8 && tile_cols == 64) bulk = tile_words<T, 8, 64>();
+  if (tile_rows == 16 && tile_cols == 64) bulk = tile_words<T, 16, 64>();
   if (tile_rows == 4 && tile_cols == 128) bulk = tile_words<T, 4, 128>();
   const int row = tile_words<T, 1, kRowChunk>();
   // Rounded to 4 words and max_n to an even count so that the FP64
@@ -1695,6 +1696,7 @@ int launch_stage(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int adv
   a.form = update_form(args);
   if (tile_rows == 8 && tile_cols == 32) return launch_stage_shape<T, 8, 32>(mem, wl, nwork, adv, max_n, a, s);
   if (tile_rows == 8 && tile_cols == 64) return launch_stage_shape<T, 8, 64>(mem, wl, nwork, adv, max_n, a, s);
+  if (tile_rows == 16 && tile_cols == 64) return launch_stage_shape<T, 16, 64>(mem, wl, nwork, adv, max_n, a, s);
   if (tile_rows == 4 && tile_cols == 128) return launch_stage_shape<T, 4, 128>(mem, wl, nwork, adv, max_n, a, s);
   return GDC_E_CONFIG;
 }

@@ -65,7 +65,7 @@ def test_fp32_compensated_vs_fp64(native):
     assert e[2] <= 1e-5, e
 
 
-@pytest.mark.parametrize("tile", [(8, 32), (8, 64), (4, 128)])
+@pytest.mark.parametrize("tile", [(8, 32), (8, 64), (4, 128), (16, 64)])
 def test_every_tile_shape_matches_oracle_on_ragged_grid(native, tile):
     """720 columns leave a ragged last column block under every tile shape
     (16, 16 and 80 columns), whose halo columns wrap to 0 and 1."""
