@@ -181,7 +181,9 @@ def time_batch(gdc, torch, members, steps, warmup, precision, ts):
     b.step(warmup)
     b.sync()
     gpt = sum(m["N"] * m["M"] * min(steps, m["nsteps"]) for m in members)
-    launches_per_step = 4 * (6 + 2) + 1
+    # per predict_correct: 3 stage launches, beta, final; 6 + 2 calls per
+    # csp2 step; then diag + diag_finalize
+    launches_per_step = 5 * (6 + 2) + 2
     active_steps = sum(min(steps, m["nsteps"]) for m in members)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
@@ -259,6 +261,16 @@ def plain_fp64(gdc, torch, ts, steps=360):
     return {"value": N * M * steps / (out[gdc.FP64][0] / 1e3), "ms": out[gdc.FP64][0],
             "fp32_value": N * M * steps / (out[gdc.FP32][0] / 1e3),
             "l2_fp32_vs_fp64": {"gd": rl2(s32[2], s64[2]), "u": rl2(s32[0], s64[0]), "v": rl2(s32[1], s64[1])}}
+
+
+def stage_traffic():
+    """DRAM bytes per stage launch from the committed ncu capture of this
+    workload (profiles/stage_kernel_f32_16x64_ensemble64.md)."""
+    try:
+        rec = json.loads((ROOT / "profiles" / "stage_kernel_f32_16x64_ensemble64.traffic.json").read_text())
+        return rec["mean_dram_bytes_per_launch"]
+    except Exception:
+        return None
 
 
 def serve_sample(gdc, ts, n=40, rate=20.0, seed=0):
@@ -405,7 +417,8 @@ def run_ours(args, rank, world, dist):
                 "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": None, "kernel": "stage_kernel<float>", "peak_source": peak_src,
+                     "traffic": stage_traffic(), "traffic_unit": "bytes per launch (ncu, mean of one predict_correct)",
+                     "kernel": "stage_kernel<float, pass, 0, 16, 64>", "peak_source": peak_src,
                      "stage_ms_per_launch": stage_ms, "bytes_per_launch": stage_bytes,
                      "kernel_ms": {"stage": prof_ms[0], "final": prof_ms[1], "diag": prof_ms[2]},
                      "kernel_launches": {"stage": prof_n[0], "final": prof_n[1], "diag": prof_n[2]},
