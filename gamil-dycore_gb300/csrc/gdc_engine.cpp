@@ -91,7 +91,24 @@ struct MemberRec {
   std::vector<int> rowinfo;
   std::vector<double> ic_u, ic_v;  // padded-layout u, v of the initial condition
   int ic_ld = 0;
+  int cutoff[20] = {};             // this member's filter cutoffs
 };
+
+// Checkpoint file (little-endian): this header, then the reference's restart
+// fields u (N x M), v (N x (M-1)), gd, ghs in FP64 (interior, lon fastest,
+// src/restart_mod.F90:63-74), then the member's exact device state in the
+// compute type: gd, iap u, iap v of its current time level, their FP32
+// compensation words (FP32 only), ghs, and the level's given u, v when the
+// level has them.
+struct RestartHeader {
+  char magic[8];  // "GDCRST01"
+  int32_t version, precision, num_lon, num_lat;
+  int64_t steps_done, nsteps;
+  double dt;
+  int32_t cutoff[20];
+  int32_t has_given, reserved;
+};
+constexpr char kRestartMagic[8] = {'G', 'D', 'C', 'R', 'S', 'T', '0', '1'};
 
 }  // namespace
 
@@ -114,6 +131,8 @@ struct BatchIface {
   virtual int profile(int n, double* ms, long long* launches) = 0;
   virtual int set_stream(void* s) = 0;
   virtual int debug_tendency(int id, int pass, double* du, double* dv, double* dgd, int ld) = 0;
+  virtual int checkpoint(int id, const char* path) = 0;
+  virtual int restore(const char* path, size_t reserve, long long nsteps_override, int* id) = 0;
   std::string err;
 };
 
@@ -201,6 +220,7 @@ class Batch final : public BatchIface {
     r.dt = dt;
     r.nsteps = nsteps;
     r.bytes = L.total;
+    for (int k = 0; k < 20; ++k) r.cutoff[k] = mp.zonal_tend_filter_cutoff_wavenumber[k];
     // Host tables.
     const Mesh mesh = make_mesh(N, M);
     const Coef co = make_coef(mesh);
@@ -339,6 +359,145 @@ class Batch final : public BatchIface {
     if (int rc = initial_diag(slot)) return rc;
     *id = slot;
     return GDC_OK;
+  }
+
+  int checkpoint(int id, const char* path) override {
+    if (!valid(id)) return fail(GDC_E_CONFIG, "checkpoint: unknown member");
+    if (!path) return fail(GDC_E_CONFIG, "checkpoint: no path");
+    const MemberRec& r = recs[id];
+    const int N = r.N, M = r.M, Mh = M - 1, ld = N + 4;
+    const size_t full = (size_t)N * M, half = (size_t)N * Mh;
+    std::vector<double> pu((size_t)ld * (M + 4)), pv((size_t)ld * (Mh + 4)), pg((size_t)ld * (M + 4));
+    if (int rc = get_state(id, pu.data(), pv.data(), pg.data(), nullptr, nullptr, nullptr, ld)) return rc;
+    const MemberDev<T>& d = hdesc[id];
+    const int lvl = r.level;
+    int uvs = -1;
+    cudaError_t e = cudaMemcpy(&uvs, d_uvslot + id, sizeof(int), cudaMemcpyDeviceToHost);
+    const bool given = uvs == lvl;
+    std::vector<std::vector<T>> raw;
+    auto take = [&](const T* src, size_t n) {
+      raw.emplace_back(n);
+      if (e == cudaSuccess) e = cudaMemcpy(raw.back().data(), src, n * sizeof(T), cudaMemcpyDeviceToHost);
+    };
+    const size_t sz[3] = {full, full, half};
+    for (int f = 0; f < 3; ++f) take(d.st[lvl][f], sz[f]);
+    if (d.lo[lvl][0])
+      for (int f = 0; f < 3; ++f) take(d.lo[lvl][f], sz[f]);
+    take(d.ghs, full);
+    if (given) {
+      take(d.given_u, full);
+      take(d.given_v, half);
+    }
+    if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("checkpoint: download", e));
+    RestartHeader h;
+    std::memset(&h, 0, sizeof(h));
+    std::memcpy(h.magic, kRestartMagic, 8);
+    h.version = 1;
+    h.precision = sizeof(T) == 4 ? GDC_FP32 : GDC_FP64;
+    h.num_lon = N;
+    h.num_lat = M;
+    h.steps_done = r.steps_done;
+    h.nsteps = r.nsteps;
+    h.dt = r.dt;
+    for (int k = 0; k < 20; ++k) h.cutoff[k] = r.cutoff[k];
+    h.has_given = given ? 1 : 0;
+    std::vector<double> ref;
+    ref.reserve(3 * full + half);
+    auto interior = [&](const std::vector<double>& a, int rows) {
+      for (int j = 0; j < rows; ++j)
+        for (int i = 0; i < N; ++i) ref.push_back(a[(size_t)(j + 2) * ld + i + 2]);
+    };
+    interior(pu, M);
+    interior(pv, Mh);
+    interior(pg, M);
+    for (size_t q = 0; q < full; ++q) ref.push_back((double)raw[h.precision == GDC_FP32 ? 6 : 3][q]);
+    FILE* fp = std::fopen(path, "wb");
+    if (!fp) return fail(GDC_E_CONFIG, std::string("checkpoint: cannot open ") + path);
+    bool ok = std::fwrite(&h, sizeof(h), 1, fp) == 1 && std::fwrite(ref.data(), sizeof(double), ref.size(), fp) == ref.size();
+    for (auto& a : raw) ok = ok && std::fwrite(a.data(), sizeof(T), a.size(), fp) == a.size();
+    ok = (std::fclose(fp) == 0) && ok;
+    return ok ? GDC_OK : fail(GDC_E_CONFIG, std::string("checkpoint: write failed: ") + path);
+  }
+
+  // Restores a checkpoint as a new member (nsteps_override >= 0 replaces the
+  // member's length): exact continuation of the checkpointed run.
+  int restore(const char* path, size_t reserve, long long nsteps_override, int* id) override {
+    if (!path || !id) return fail(GDC_E_CONFIG, "restore: no path or id");
+    FILE* fp = std::fopen(path, "rb");
+    if (!fp) return fail(GDC_E_CONFIG, std::string("restore: cannot open ") + path);
+    RestartHeader h;
+    auto bad = [&](const std::string& m) {
+      std::fclose(fp);
+      return fail(GDC_E_CONFIG, "restore: " + m);
+    };
+    if (std::fread(&h, sizeof(h), 1, fp) != 1 || std::memcmp(h.magic, kRestartMagic, 8) != 0 || h.version != 1)
+      return bad("not a checkpoint file");
+    if (h.precision != (sizeof(T) == 4 ? GDC_FP32 : GDC_FP64))
+      return bad("checkpoint precision differs from the batch's");
+    const int N = h.num_lon, M = h.num_lat;
+    if (N < 8 || M < 5 || N % 4 != 0 || N > (1 << 16) || M > (1 << 16) || h.steps_done < 0)
+      return bad("invalid grid in header");
+    const int Mh = M - 1, ld = N + 4;
+    const size_t full = (size_t)N * M, half = (size_t)N * Mh;
+    std::vector<double> ref(3 * full + half);
+    if (std::fread(ref.data(), sizeof(double), ref.size(), fp) != ref.size()) return bad("truncated file");
+    const bool fp32 = sizeof(T) == 4;
+    const size_t sz[3] = {full, full, half};
+    std::vector<std::vector<T>> raw;
+    auto take = [&](size_t n) {
+      raw.emplace_back(n);
+      return std::fread(raw.back().data(), sizeof(T), n, fp) == n;
+    };
+    bool ok = true;
+    for (int f = 0; f < 3; ++f) ok = ok && take(sz[f]);
+    if (fp32)
+      for (int f = 0; f < 3; ++f) ok = ok && take(sz[f]);
+    ok = ok && take(full);
+    if (h.has_given) ok = ok && take(full) && take(half);
+    if (!ok) return bad("truncated file");
+    std::fclose(fp);
+    // Admit with the reference fields, then put the exact state in place.
+    std::vector<double> pu((size_t)ld * (M + 4), 0.0), pv((size_t)ld * (Mh + 4), 0.0), pg(pu.size(), 0.0),
+        ph(pu.size(), 0.0);
+    const double* src = ref.data();
+    auto pad = [&](std::vector<double>& a, int rows) {
+      for (int j = 0; j < rows; ++j)
+        for (int i = 0; i < N; ++i) a[(size_t)(j + 2) * ld + i + 2] = *src++;
+    };
+    pad(pu, M);
+    pad(pv, Mh);
+    pad(pg, M);
+    pad(ph, M);
+    const long long nsteps = nsteps_override >= 0 ? nsteps_override : h.nsteps;
+    if (int rc = add(N, M, h.dt, nsteps, h.cutoff, pu.data(), pv.data(), pg.data(), ph.data(), ld, reserve, id))
+      return rc;
+    MemberRec& r = recs[*id];
+    const MemberDev<T>& d = hdesc[*id];
+    const int lvl = r.level;
+    cudaError_t e = cudaSuccess;
+    auto put = [&](T* dst, const std::vector<T>& a) {
+      if (e == cudaSuccess) e = cudaMemcpy(dst, a.data(), a.size() * sizeof(T), cudaMemcpyHostToDevice);
+    };
+    int q = 0;
+    for (int f = 0; f < 3; ++f) put(d.st[lvl][f], raw[q++]);
+    if (fp32)
+      for (int f = 0; f < 3; ++f) put(d.lo[lvl][f], raw[q++]);
+    put(d.ghs, raw[q++]);
+    int uvs = -1;
+    if (h.has_given) {
+      put(d.given_u, raw[q++]);
+      put(d.given_v, raw[q++]);
+      uvs = lvl;
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(d_uvslot + *id, &uvs, sizeof(int), cudaMemcpyHostToDevice);
+    const long long done = h.steps_done;
+    if (e == cudaSuccess) e = cudaMemcpy(d_steps + *id, &done, sizeof(done), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("restore: upload", e));
+    r.steps_done = done;
+    r.active = done < r.nsteps;
+    r.finished = !r.active;
+    dirty = true;
+    return initial_diag(*id);  // the diagnostics of the restored state
   }
 
   int remove(int id) override {
@@ -1365,6 +1524,12 @@ int gdc_batch_diag(gdc_batch* b, int id, double* m, double* e, double* beta) {
 }
 int gdc_batch_active(gdc_batch* b, int* n) { return (b && n) ? b->impl->active(n) : GDC_E_CONFIG; }
 int gdc_batch_set_tile(gdc_batch* b, int r, int c) { return b ? b->impl->set_tile(r, c) : GDC_E_CONFIG; }
+int gdc_batch_checkpoint(gdc_batch* b, int member_id, const char* path) {
+  return b ? b->impl->checkpoint(member_id, path) : GDC_E_CONFIG;
+}
+int gdc_batch_restore(gdc_batch* b, const char* path, size_t reserve_bytes, int* member_id) {
+  return b ? b->impl->restore(path, reserve_bytes, -1, member_id) : GDC_E_CONFIG;
+}
 int gdc_batch_autotune(gdc_batch* b, int* r, int* c, double* ms) {
   return b ? b->impl->autotune(r, c, ms) : GDC_E_CONFIG;
 }
@@ -1500,6 +1665,29 @@ int gdc_diag(gdc_handle* h, double* m, double* e, double* beta) {
     return GDC_E_STATE;
   }
   return h->b->impl->diag(h->id, m, e, beta);
+}
+
+int gdc_write_restart(gdc_handle* h, const char* path) {
+  if (!h) return GDC_E_CONFIG;
+  h->err.clear();
+  if (h->id < 0) {
+    h->err = "gdc_write_restart before gdc_set_state";
+    return GDC_E_STATE;
+  }
+  return h->b->impl->checkpoint(h->id, path);
+}
+
+int gdc_read_restart(gdc_handle* h, const char* path) {
+  if (!h) return GDC_E_CONFIG;
+  h->err.clear();
+  if (h->id >= 0) {
+    gdc_batch_remove(h->b, h->id);
+    h->id = -1;
+  }
+  int id = -1;
+  const int rc = h->b->impl->restore(path, 0, (1LL << 62), &id);
+  if (rc == GDC_OK) h->id = id;
+  return rc;
 }
 
 int gdc_steps_done(gdc_handle* h, long long* steps) {

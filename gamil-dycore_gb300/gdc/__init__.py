@@ -124,6 +124,10 @@ def lib() -> ctypes.CDLL:
             "gdc_batch_diag": (ctypes.c_int, [vp, ctypes.c_int, dp, dp, dp]),
             "gdc_batch_active": (ctypes.c_int, [vp, ip]),
             "gdc_batch_set_tile": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
+            "gdc_batch_checkpoint": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_char_p]),
+            "gdc_batch_restore": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_size_t, ip]),
+            "gdc_write_restart": (ctypes.c_int, [vp, ctypes.c_char_p]),
+            "gdc_read_restart": (ctypes.c_int, [vp, ctypes.c_char_p]),
             "gdc_batch_autotune": (ctypes.c_int, [vp, ip, ip, dp]),
             "gdc_batch_profile": (ctypes.c_int, [vp, ctypes.c_int, dp, i64p]),
             "gdc_algorithmic_bytes_per_gpt_step": (ctypes.c_double, [ctypes.POINTER(Params)]),
@@ -296,6 +300,12 @@ class Model:
         self._check(lib().gdc_debug_tendency(self.h, pass_, _ptr(du), _ptr(dv), _ptr(dgd), self.N + 4))
         return du, dv, dgd
 
+    def write_restart(self, path: str):
+        self._check(lib().gdc_write_restart(self.h, str(path).encode()))
+
+    def read_restart(self, path: str):
+        self._check(lib().gdc_read_restart(self.h, str(path).encode()))
+
     def set_stream(self, cuda_stream: int | None):
         self._check(lib().gdc_set_stream(self.h, ctypes.c_void_p(cuda_stream) if cuda_stream else None))
 
@@ -386,6 +396,19 @@ class Batch:
         n = ctypes.c_int()
         self._check(lib().gdc_batch_active(self.b, ctypes.byref(n)))
         return n.value
+
+    def checkpoint(self, mid: int, path: str):
+        self._check(lib().gdc_batch_checkpoint(self.b, mid, str(path).encode()))
+
+    def restore(self, path: str, reserve_bytes: int = 0) -> int:
+        """Admit a checkpoint as a new member; returns its id."""
+        mid = ctypes.c_int()
+        self._check(lib().gdc_batch_restore(self.b, str(path).encode(), reserve_bytes, ctypes.byref(mid)))
+        with open(path, "rb") as f:
+            hdr = f.read(24)
+        N, M = int.from_bytes(hdr[16:20], "little"), int.from_bytes(hdr[20:24], "little")
+        self.grids[mid.value] = (N, M)
+        return mid.value
 
     def set_tile(self, rows: int, cols: int):
         self._check(lib().gdc_batch_set_tile(self.b, rows, cols))

@@ -132,8 +132,14 @@ int gdc_get_iap(gdc_handle* h, double* iap_u, double* iap_v, double* iap_gd,
  * logged by log_add_diag('beta') (src/dycore_mod.F90:787, :747). */
 int gdc_diag(gdc_handle* h, double* total_mass, double* total_energy,
              double* beta);
-/* Steps completed since set_state. */
+/* Steps completed since set_state (or since the checkpointed run began). */
 int gdc_steps_done(gdc_handle* h, long long* steps);
+/* restart_write / restart_read + dycore_restart (src/restart_mod.F90:41-75,
+ * src/dycore_mod.F90:113-117): the checkpoint format of
+ * gdc_batch_checkpoint; reading replaces the current state and continues
+ * the checkpointed run exactly. */
+int gdc_write_restart(gdc_handle* h, const char* path);
+int gdc_read_restart(gdc_handle* h, const char* path);
 
 /* space_operators(state(old), tend, pass) (src/dycore_mod.F90:184-365)
  * including the filter rescale; du/dv/dgd returned in the padded layout.
@@ -234,6 +240,17 @@ int gdc_batch_remove(gdc_batch* b, int member_id);
  * stop at their own length).  Enqueue only. */
 int gdc_batch_step(gdc_batch* b, int nsteps);
 int gdc_batch_sync(gdc_batch* b);
+/* Checkpoint of one member to `path` and its exact continuation: the file
+ * holds the reference's restart fields u, v, gd, ghs (FP64; replaces
+ * restart_write, src/restart_mod.F90:60-75) and the member's device state
+ * (the current time level in the compute type with its FP32 compensation
+ * words, ghs, the level's given u, v), so a restored member continues
+ * bitwise as if never interrupted.  The batch's precision must match the
+ * file's.  gdc_batch_restore admits the checkpoint as a new member
+ * (admission by free memory as gdc_batch_add) with its steps done and
+ * length. */
+int gdc_batch_checkpoint(gdc_batch* b, int member_id, const char* path);
+int gdc_batch_restore(gdc_batch* b, const char* path, size_t reserve_bytes, int* member_id);
 /* Per-member status: steps done, finished flag, NaN step (-1 if none). */
 int gdc_batch_member_info(gdc_batch* b, int member_id, long long* steps_done,
                           int* finished, long long* nan_step);
