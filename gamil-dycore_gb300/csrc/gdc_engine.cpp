@@ -132,6 +132,7 @@ struct BatchIface {
   virtual int set_stream(void* s) = 0;
   virtual int debug_tendency(int id, int pass, double* du, double* dv, double* dgd, int ld) = 0;
   virtual int checkpoint(int id, const char* path) = 0;
+  virtual int history(int id, double* ua, double* va, double* gh, double* div, double* vor, int ld) = 0;
   virtual int restore(const char* path, size_t reserve, long long nsteps_override, int* id) = 0;
   std::string err;
 };
@@ -417,6 +418,51 @@ class Batch final : public BatchIface {
     for (auto& a : raw) ok = ok && std::fwrite(a.data(), sizeof(T), a.size(), fp) == a.size();
     ok = (std::fclose(fp) == 0) && ok;
     return ok ? GDC_OK : fail(GDC_E_CONFIG, std::string("checkpoint: write failed: ") + path);
+  }
+
+  int history(int id, double* ua, double* va, double* gh, double* div, double* vor, int ld) override {
+    if (!valid(id)) return fail(GDC_E_CONFIG, "history: unknown member");
+    const MemberRec& r = recs[id];
+    const int N = r.N, M = r.M, Mh = M - 1;
+    if (ld < N + 4) return fail(GDC_E_CONFIG, "history: ld < num_lon + 4");
+    sync_stream();
+    const int lvl = level_of(id);
+    int uvs = -1;
+    cudaError_t e = cudaMemcpy(&uvs, d_uvslot + id, sizeof(int), cudaMemcpyDeviceToHost);
+    const size_t full = (size_t)N * M;
+    double* buf = nullptr;
+    if (e == cudaSuccess) e = cudaMalloc(&buf, 5 * full * sizeof(double));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(GDC_E_OOM, cuda_msg("history: buffers", e));
+    }
+    int rc = launch_history<T>(d_mem, id, lvl, uvs == lvl ? 1 : 0, M, buf, buf + full, buf + 2 * full,
+                               buf + 3 * full, buf + 4 * full, stream);
+    std::vector<double> h(5 * full);
+    if (rc == GDC_OK) e = cudaMemcpyAsync(h.data(), buf, h.size() * sizeof(double), cudaMemcpyDeviceToHost, stream);
+    if (rc == GDC_OK && e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    cudaFree(buf);
+    if (rc) return fail(rc, "history: launch failed");
+    if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("history", e));
+    auto put = [&](double* f, int k, int rows) {
+      if (!f) return;
+      std::memset(f, 0, sizeof(double) * (size_t)ld * (rows + 4));
+      for (int j = 0; j < rows; ++j)
+        for (int i = 0; i < N; ++i) f[(size_t)(j + 2) * ld + i + 2] = h[k * full + (size_t)j * N + i];
+      for (int j = 0; j < rows + 4; ++j) {  // periodic longitude halo
+        double* row = f + (size_t)j * ld;
+        row[0] = row[N];
+        row[1] = row[N + 1];
+        row[N + 2] = row[2];
+        row[N + 3] = row[3];
+      }
+    };
+    put(ua, 0, M);
+    put(va, 1, M);
+    put(gh, 2, M);
+    put(div, 3, M);
+    put(vor, 4, Mh);
+    return GDC_OK;
   }
 
   // Restores a checkpoint as a new member (nsteps_override >= 0 replaces the
@@ -1524,6 +1570,10 @@ int gdc_batch_diag(gdc_batch* b, int id, double* m, double* e, double* beta) {
 }
 int gdc_batch_active(gdc_batch* b, int* n) { return (b && n) ? b->impl->active(n) : GDC_E_CONFIG; }
 int gdc_batch_set_tile(gdc_batch* b, int r, int c) { return b ? b->impl->set_tile(r, c) : GDC_E_CONFIG; }
+int gdc_batch_history(gdc_batch* b, int member_id, double* u_a, double* v_a, double* gh, double* div, double* vor,
+                      int ld) {
+  return b ? b->impl->history(member_id, u_a, v_a, gh, div, vor, ld) : GDC_E_CONFIG;
+}
 int gdc_batch_checkpoint(gdc_batch* b, int member_id, const char* path) {
   return b ? b->impl->checkpoint(member_id, path) : GDC_E_CONFIG;
 }
@@ -1665,6 +1715,16 @@ int gdc_diag(gdc_handle* h, double* m, double* e, double* beta) {
     return GDC_E_STATE;
   }
   return h->b->impl->diag(h->id, m, e, beta);
+}
+
+int gdc_history(gdc_handle* h, double* u_a, double* v_a, double* gh, double* div, double* vor, int ld) {
+  if (!h) return GDC_E_CONFIG;
+  h->err.clear();
+  if (h->id < 0) {
+    h->err = "gdc_history before gdc_set_state";
+    return GDC_E_STATE;
+  }
+  return h->b->impl->history(h->id, u_a, v_a, gh, div, vor, ld);
 }
 
 int gdc_write_restart(gdc_handle* h, const char* path) {

@@ -267,6 +267,11 @@ int launch_copy_state(const MemberDev<T>* mem, const WorkItem* wl, int nwork, in
 template <typename T>
 int launch_stage_strips(const MemberDev<T>* mem, const WorkItem* strips, int nstrip, int adv, const StageArgs& a,
                         void* stream);
+// History output of member `slot` at level `lvl` into device FP64 buffers
+// (num_lat x num_lon each; vor num_lat - 1 rows).
+template <typename T>
+int launch_history(const MemberDev<T>* mem, int slot, int lvl, int given, int num_lat, double* ua, double* va,
+                   double* gh, double* div, double* vor, void* stream);
 // Shared-memory bytes of one stage launch.
 template <typename T>
 size_t stage_smem_bytes(int tile_rows, int tile_cols, int max_n, int* staging_words);

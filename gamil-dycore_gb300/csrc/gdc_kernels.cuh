@@ -1627,6 +1627,77 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// ------------------------------------------------------------ history
+// History output of one member's state(old) in FP64 (src/history_mod.F90:
+// 101-108 and diag_run's div, vor, src/diag_mod.F90:49-68): u, v on the A
+// grid, gh = gd + ghs, divergence on full rows 1..M-2 (0 on the pole rows),
+// vorticity on half rows.  u, v are the level's given ones or recovered as
+// update_state does (src/dycore_mod.F90:636-645); FP32 levels are read as
+// hi + lo.  One block per full row.
+
+template <typename T>
+__device__ inline double hist_val(const T* hi, const T* lo, size_t o) {
+  double v = (double)hi[o];
+  if (lo) v += (double)lo[o];
+  return v;
+}
+
+template <typename T>
+__device__ inline double hist_u(const MemberDev<T>& md, int lvl, bool given, int i, int j) {
+  const int N = md.N, M = md.M;
+  if (j < 0 || j >= M) return 0.0;  // zero latitude halo
+  i = i < 0 ? i + N : (i >= N ? i - N : i);
+  const size_t o = (size_t)j * N + i;
+  if (given) return (double)md.given_u[o];
+  if (j == 0 || j == M - 1) return 0.0;
+  const size_t oe = (size_t)j * N + (i + 1 < N ? i + 1 : 0);
+  const double g0 = sqrt(hist_val(md.st[lvl][F_GD], md.lo[lvl][F_GD], o));
+  const double g1 = sqrt(hist_val(md.st[lvl][F_GD], md.lo[lvl][F_GD], oe));
+  return hist_val(md.st[lvl][F_IU], md.lo[lvl][F_IU], o) * 2.0 / (g0 + g1);
+}
+
+template <typename T>
+__device__ inline double hist_v(const MemberDev<T>& md, int lvl, bool given, int i, int jh) {
+  const int N = md.N, Mh = md.Mh;
+  if (jh < 0 || jh >= Mh) return 0.0;
+  i = i < 0 ? i + N : (i >= N ? i - N : i);
+  const size_t o = (size_t)jh * N + i;
+  if (given) return (double)md.given_v[o];
+  const double g0 = sqrt(hist_val(md.st[lvl][F_GD], md.lo[lvl][F_GD], o));
+  const double g1 = sqrt(hist_val(md.st[lvl][F_GD], md.lo[lvl][F_GD], o + N));
+  return hist_val(md.st[lvl][F_IV], md.lo[lvl][F_IV], o) * 2.0 / (g0 + g1);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    history_kernel(const MemberDev<T>* __restrict__ mems, int slot, int lvl, int given, double* ua, double* va,
+                   double* gh, double* div, double* vor) {
+  const MemberDev<T>& md = mems[slot];
+  const int N = md.N, M = md.M, Mh = md.Mh;
+  const int j = blockIdx.x;
+  const bool gv = given != 0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const size_t o = (size_t)j * N + i;
+    const double uc = hist_u(md, lvl, gv, i, j), uw = hist_u(md, lvl, gv, i - 1, j);
+    const double vc = hist_v(md, lvl, gv, i, j), vs = hist_v(md, lvl, gv, i, j - 1);
+    ua[o] = 0.5 * (uc + uw);
+    va[o] = 0.5 * (vc + vs);
+    gh[o] = hist_val(md.st[lvl][F_GD], md.lo[lvl][F_GD], o) + (double)md.ghs[o];
+    double d = 0.0;
+    if (j >= 1 && j <= M - 2) {
+      const double vm1 = vs * (double)ch(md, CH_COS, j - 1);
+      const double vp1 = vc * (double)ch(md, CH_COS, j);
+      d = (uc - uw) / (double)cf(md, CF_DLON, j) + (vp1 - vm1) / (double)cf(md, CF_DLAT, j);
+    }
+    div[o] = d;
+    if (j < Mh) {
+      const double vm1 = vc, vp1 = hist_v(md, lvl, gv, i + 1, j);
+      const double um1 = uc, up1 = hist_u(md, lvl, gv, i, j + 1);
+      vor[o] = (vp1 - vm1) / (double)ch(md, CH_DLON, j) - (up1 - um1) / (double)ch(md, CH_DLAT, j);
+    }
+  }
+}
+
 // --------------------------------------------------------- launchers
 
 static inline int check_launch() {
@@ -1726,6 +1797,13 @@ int launch_stage_strips(const MemberDev<T>* mem, const WorkItem* strips, int nst
   GDC_DISPATCH(kSlowPass, GDC_ADV_UPWIND)
 #undef GDC_DISPATCH
   return GDC_E_CONFIG;
+}
+
+template <typename T>
+int launch_history(const MemberDev<T>* mem, int slot, int lvl, int given, int num_lat, double* ua, double* va,
+                   double* gh, double* div, double* vor, void* stream) {
+  history_kernel<T><<<num_lat, kThreads, 0, (cudaStream_t)stream>>>(mem, slot, lvl, given, ua, va, gh, div, vor);
+  return check_launch();
 }
 
 template <typename T>

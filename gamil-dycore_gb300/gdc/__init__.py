@@ -127,6 +127,8 @@ def lib() -> ctypes.CDLL:
             "gdc_batch_checkpoint": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_char_p]),
             "gdc_batch_restore": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_size_t, ip]),
             "gdc_write_restart": (ctypes.c_int, [vp, ctypes.c_char_p]),
+            "gdc_history": (ctypes.c_int, [vp, dp, dp, dp, dp, dp, ctypes.c_int]),
+            "gdc_batch_history": (ctypes.c_int, [vp, ctypes.c_int, dp, dp, dp, dp, dp, ctypes.c_int]),
             "gdc_read_restart": (ctypes.c_int, [vp, ctypes.c_char_p]),
             "gdc_batch_autotune": (ctypes.c_int, [vp, ip, ip, dp]),
             "gdc_batch_profile": (ctypes.c_int, [vp, ctypes.c_int, dp, i64p]),
@@ -300,6 +302,13 @@ class Model:
         self._check(lib().gdc_debug_tendency(self.h, pass_, _ptr(du), _ptr(dv), _ptr(dgd), self.N + 4))
         return du, dv, dgd
 
+    def history(self):
+        """A-grid u, v, gh = gd + ghs, divergence and vorticity of state(old)."""
+        N, M = self.N, self.M
+        out = [padded(M, N) for _ in range(4)] + [padded(M - 1, N)]
+        self._check(lib().gdc_history(self.h, *map(_ptr, out), N + 4))
+        return dict(zip(("u_a", "v_a", "gh", "div", "vor"), out))
+
     def write_restart(self, path: str):
         self._check(lib().gdc_write_restart(self.h, str(path).encode()))
 
@@ -396,6 +405,13 @@ class Batch:
         n = ctypes.c_int()
         self._check(lib().gdc_batch_active(self.b, ctypes.byref(n)))
         return n.value
+
+    def history(self, mid: int):
+        """A-grid u, v, gh = gd + ghs, divergence and vorticity of a member."""
+        N, M = self.grids[mid]
+        out = [padded(M, N) for _ in range(4)] + [padded(M - 1, N)]
+        self._check(lib().gdc_batch_history(self.b, mid, *map(_ptr, out), N + 4))
+        return dict(zip(("u_a", "v_a", "gh", "div", "vor"), out))
 
     def checkpoint(self, mid: int, path: str):
         self._check(lib().gdc_batch_checkpoint(self.b, mid, str(path).encode()))

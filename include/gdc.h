@@ -140,6 +140,12 @@ int gdc_steps_done(gdc_handle* h, long long* steps);
  * the checkpointed run exactly. */
 int gdc_write_restart(gdc_handle* h, const char* path);
 int gdc_read_restart(gdc_handle* h, const char* path);
+/* History output of state(old), computed on the device in FP64
+ * (history_write_state, src/history_mod.F90:93-124, with diag_run's div and
+ * vor, src/diag_mod.F90:49-68): u, v averaged to the A grid, gh = gd + ghs,
+ * divergence (pole rows 0) and relative vorticity.  Padded layout, any
+ * pointer may be NULL: u_a, v_a, gh, div num_lat rows, vor num_lat - 1. */
+int gdc_history(gdc_handle* h, double* u_a, double* v_a, double* gh, double* div, double* vor, int ld);
 
 /* space_operators(state(old), tend, pass) (src/dycore_mod.F90:184-365)
  * including the filter rescale; du/dv/dgd returned in the padded layout.
@@ -250,6 +256,9 @@ int gdc_batch_sync(gdc_batch* b);
  * (admission by free memory as gdc_batch_add) with its steps done and
  * length. */
 int gdc_batch_checkpoint(gdc_batch* b, int member_id, const char* path);
+/* gdc_history for one member of a batch. */
+int gdc_batch_history(gdc_batch* b, int member_id, double* u_a, double* v_a, double* gh, double* div,
+                      double* vor, int ld);
 int gdc_batch_restore(gdc_batch* b, const char* path, size_t reserve_bytes, int* member_id);
 /* Per-member status: steps done, finished flag, NaN step (-1 if none). */
 int gdc_batch_member_info(gdc_batch* b, int member_id, long long* steps_done,

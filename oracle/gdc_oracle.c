@@ -1050,6 +1050,39 @@ void gdo_tendency(gdo_model* m, int pass, double* du, double* dv, double* dgd) {
   if (dgd) memcpy(dgd, t->a[T_DGD], full_sz(m) * sizeof(double));
 }
 
+/* history_write_state's A-grid wind and gh (src/history_mod.F90:101-108) and
+ * diag_run's div and vor (src/diag_mod.F90:49-68) of state(old), in the
+ * padded layout (halos 0).  div is left 0 on the pole rows, as the reference
+ * never assigns them. */
+void gdo_history(const gdo_model* m, double* ua, double* va, double* gh, double* div, double* vor) {
+  const int N = m->N, M = m->M, Mh = m->Mh;
+  const state_t* s = &m->state_mem[m->old + 1];
+  memset(ua, 0, full_sz(m) * sizeof(double));
+  memset(va, 0, full_sz(m) * sizeof(double));
+  memset(gh, 0, full_sz(m) * sizeof(double));
+  memset(div, 0, full_sz(m) * sizeof(double));
+  memset(vor, 0, half_sz(m) * sizeof(double));
+  for (int j = 1; j <= M; ++j)
+    for (int i = 1; i <= N; ++i) {
+      AT(m, ua, i, j) = 0.5 * (AT(m, s->u, i, j) + AT(m, s->u, i - 1, j));
+      AT(m, va, i, j) = 0.5 * (AT(m, s->v, i, j) + AT(m, s->v, i, j - 1));
+      AT(m, gh, i, j) = AT(m, s->gd, i, j) + AT(m, m->ghs, i, j);
+    }
+  for (int j = 2; j <= M - 1; ++j)
+    for (int i = 1; i <= N; ++i) {
+      const double um1 = AT(m, s->u, i - 1, j), up1 = AT(m, s->u, i, j);
+      const double vm1 = AT(m, s->v, i, j - 1) * m->half_cos[j - 1];
+      const double vp1 = AT(m, s->v, i, j) * m->half_cos[j];
+      AT(m, div, i, j) = (up1 - um1) / m->full_dlon[j] + (vp1 - vm1) / m->full_dlat[j];
+    }
+  for (int j = 1; j <= Mh; ++j)
+    for (int i = 1; i <= N; ++i) {
+      const double um1 = AT(m, s->u, i, j), up1 = AT(m, s->u, i, j + 1);
+      const double vm1 = AT(m, s->v, i, j), vp1 = AT(m, s->v, i + 1, j);
+      AT(m, vor, i, j) = (vp1 - vm1) / m->half_dlon[j] - (up1 - um1) / m->half_dlat[j];
+    }
+}
+
 /* src/dycore_mod.F90:794-851 (disabled in the reference, :363). */
 void gdo_antisymmetry(const gdo_model* m, double* out4) {
   int N = m->N, M = m->M, Mh = m->Mh;

@@ -61,6 +61,9 @@ void gdo_diag(const gdo_model* m, double* total_mass, double* total_energy,
 /* Operator-level access used by the unit parity tests:
  * space_operators(state(old), tend(0), pass) and its du/dv/dgd. */
 void gdo_tendency(gdo_model* m, int pass, double* du, double* dv, double* dgd);
+/* History fields of state(old): A-grid u, v, gh = gd + ghs, div, vor
+ * (padded layout; vor has num_lat - 1 rows). */
+void gdo_history(const gdo_model* m, double* ua, double* va, double* gh, double* div, double* vor);
 /* The four antisymmetry sums of check_antisymmetry for tend(0). */
 void gdo_antisymmetry(const gdo_model* m, double* out4);
 /* Filter one padded row x in place with the factors of a full (half=0) or

@@ -40,6 +40,7 @@ def lib(fast: bool = False) -> ctypes.CDLL:
         L.gdo_diag.argtypes = [vp, dp, dp, dp]
         L.gdo_tendency.argtypes = [vp, i, dp, dp, dp]
         L.gdo_antisymmetry.argtypes = [vp, dp]
+        L.gdo_history.argtypes = [vp, dp, dp, dp, dp, dp]
         L.gdo_filter_row.argtypes = [vp, i, i, dp]
         L.gdo_filter_flags.argtypes = [vp, ip, ip, ip, ip]
         _lib = L
@@ -103,6 +104,14 @@ class OracleModel:
         iu, iv, ig = _pad(M, N), _pad(M - 1, N), _pad(M, N)
         self._L.gdo_get_state(self.h, _ptr(u), _ptr(v), _ptr(gd), _ptr(iu), _ptr(iv), _ptr(ig))
         return dict(u=u, v=v, gd=gd, iu=iu, iv=iv, ig=ig)
+
+    def history(self):
+        """A-grid u, v, gh, div, vor of state(old) (padded layout)."""
+        N, M = self.N, self.M
+        ua, va, gh, dv = _pad(M, N), _pad(M, N), _pad(M, N), _pad(M, N)
+        vo = _pad(M - 1, N)
+        self._L.gdo_history(self.h, _ptr(ua), _ptr(va), _ptr(gh), _ptr(dv), _ptr(vo))
+        return dict(u_a=ua, v_a=va, gh=gh, div=dv, vor=vo)
 
     def diag(self):
         m, e, b = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()

@@ -150,3 +150,27 @@ def test_steady_geostrophic_stays_steady():
     s = o.get_state()
     err = np.sqrt(np.mean((interior(s["gd"]) - interior(gd)) ** 2)) / np.mean(interior(gd))
     assert err < 1e-3, err  # truncation error of a 5-degree grid after 4 hours
+
+
+def test_history_fields_known_answers():
+    """A-grid wind, gh, div and vor of the oracle (src/history_mod.F90:101-108,
+    src/diag_mod.F90:49-68) on the seeded state: its u, v come from a
+    streamfunction differenced at C-grid corners, so the discrete divergence
+    vanishes; the vorticity is that streamfunction's discrete Laplacian-like
+    field (nonzero); u is 0 on the pole rows; gh = gd + ghs exactly."""
+    N, M = 72, 37
+    u, v, gd, ghs = _seeded(N, M, seed=4)
+    o = OracleModel(N, M, 600.0, subcycles=4, split_scheme=2, cutoff=[4])
+    o.set_state(u, v, gd, ghs)
+    h = o.history()
+    a, dlon = 6.37122e6, 2 * np.pi / N
+    scale = np.abs(u).max() / (a * dlon)
+    assert np.abs(h["div"]).max() < 1e-12 * scale
+    assert np.abs(interior(h["vor"])).max() > 1e-3 * scale
+    assert np.array_equal(interior(h["gh"]), interior(gd) + interior(ghs))
+    assert np.all(h["u_a"][2] == 0) and np.all(h["u_a"][M + 1] == 0)
+    # A-grid averages: interior columns and the periodic wrap
+    assert np.array_equal(h["u_a"][5, 3:N + 2], 0.5 * (u[5, 3:N + 2] + u[5, 2:N + 1]))
+    assert h["u_a"][5, 2] == 0.5 * (u[5, 2] + u[5, N + 1])
+    assert np.array_equal(h["v_a"][2, 2:N + 2], 0.5 * v[2, 2:N + 2])          # south pole row
+    assert np.array_equal(h["v_a"][M + 1, 2:N + 2], 0.5 * v[M, 2:N + 2])      # north pole row
