@@ -168,6 +168,7 @@ class Batch final : public BatchIface {
     hdesc.resize(kSlots);
     std::memset(hdesc.data(), 0, sizeof(MemberDev<T>) * kSlots);
     set_tile(0, 0);
+    cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, P.device);
     e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("init", e));
     return GDC_OK;
@@ -902,6 +903,11 @@ class Batch final : public BatchIface {
   int nrow = 0;                  // whole-row tasks at the head of the work list
   int tile_r = 8, tile_c = 32;   // tile shape, or band rows x kStripCols
   bool strips = false;           // work list of warp strips instead of tiles
+  // Whole-row tasks split by field: in FP64 (a row's filters are long FP64
+  // work) or when the batch has few tiles per SM (the row tasks are then the
+  // critical path); otherwise one task per row stages the row once.
+  bool split_rows = sizeof(T) == 8;
+  int num_sms = 152;
   // With strips, the whole-row tasks run on a second stream, concurrently
   // with the strips over the ordinary rows.
   cudaStream_t side = nullptr;
@@ -918,9 +924,9 @@ class Batch final : public BatchIface {
   std::vector<void*> allocs;
 
   // Fastest measured: FP32 16x64 tiles on the 64-member ensemble, FP64
-  // 8x64 on the single 360x181 member.
+  // 8x32 on the single 360x181 member.
   static int default_rows() { return sizeof(T) == 4 ? 16 : 8; }
-  static int default_cols() { return 64; }
+  static int default_cols() { return sizeof(T) == 4 ? 64 : 32; }
 
   // The diffusion and copy kernels run on 8x32, 8x64 or 4x128 tiles.
   bool own_tile_list() const {
@@ -1023,7 +1029,17 @@ class Batch final : public BatchIface {
     int pbase = pcount;
     // Whole-row tasks first (they are the longest items).
     for (int j = 0; j < M; ++j)
-      if (r.rowinfo[j] & RI_SPECIAL) out.push_back(WorkItem{s, 1, j, 0, 1, N, pcount++, 0});
+      if (r.rowinfo[j] & RI_SPECIAL) {
+        if (split_rows) {
+          // one task per field (no iap v on the north pole row): a row's
+          // filters then run on three SMs
+          for (int f : {F_GD, F_IU, F_IV})
+            if (f != F_IV || j < M - 1) out.push_back(WorkItem{s, 1, j, 0, 1, N, pcount++, f});
+        } else {
+          // one task for the three fields (the row is staged once)
+          out.push_back(WorkItem{s, 1, j, 0, 1, N, pcount++, -1});
+        }
+      }
     // Bulk tiles over runs of ordinary rows.
     int j = 0;
     while (j < M) {
@@ -1059,6 +1075,15 @@ class Batch final : public BatchIface {
     std::vector<WorkItem> rows_first, tiles;
     int pc = 0;
     max_n = 8;
+    {
+      long long ntiles = 0;  // bulk items of the layout, to pick the row-task form
+      for (int s = 0; s < kSlots; ++s) {
+        if (!recs[s].used || !recs[s].active) continue;
+        const long long cols = strips ? (recs[s].N + kStripCols - 1) / kStripCols : (recs[s].N + tile_c - 1) / tile_c;
+        ntiles += cols * ((recs[s].M + tile_r - 1) / tile_r);
+      }
+      split_rows = sizeof(T) == 8 || ntiles < 8LL * num_sms;
+    }
     for (int s = 0; s < kSlots; ++s) {
       if (!recs[s].used || !recs[s].active) continue;
       active_slots.push_back(s);

@@ -145,7 +145,7 @@ struct WorkItem {
   int rows;    // tile rows
   int cols;    // tile columns
   int pidx;    // partial-sum slot
-  int pad;
+  int field;   // whole-row task: the one field it computes (F_GD, F_IU, F_IV), or -1 for all three
 };
 
 // What a stage launch does with the tendency T = space_operators(in):

@@ -976,47 +976,43 @@ __device__ __forceinline__ void strip_item(const MemberDev<T>& md, const WorkIte
     strip_warp<T, PASS, ADV, UF, false>(md, w, a);
 }
 
-// The end of a whole-row task once the row's raw tendencies are in shared
-// memory (rdu, rdv, rdg; N each): the pole cap of dgd (from the FP64 sum
-// `cap` of this block), the zonal filters, and the update.
+// The end of a whole-row task for field f once the row's raw tendency is in
+// shared memory (x, N values): the pole cap of dgd (from the FP64 sum `cap`
+// of this block), the zonal filter of that field, and its update.
 template <typename T, int PASS>
-__device__ void row_tail(const MemberDev<T>& md, const StageArgs& a, Emit<T>& em, int j, T* rdu, T* rdv, T* rdg,
+__device__ void row_tail(const MemberDev<T>& md, const StageArgs& a, Emit<T>& em, int j, int f, T* x,
                          const Acc<double>& cap, T* coefs, T* redT, const T* gd_in, const T* iu_in,
                          const T* iv_in, const T* tw) {
   const int N = md.N, M = md.M, Mh = md.Mh;
   const int info = md.rowinfo[j];
   const bool has_du = (j >= 1 && j <= M - 2);
-  const bool has_dv = (j <= Mh - 1);
   const bool south = (j == 0), north = (j == M - 1);
-  if ((south || north) && PASS != kSlowPass) {
+  if (f == F_GD && (south || north) && PASS != kSlowPass) {
     double* redD = reinterpret_cast<double*>(redT + 64);
     double s = block_value(cap, redD);
     if (north) s = -s;
     s = s * 2.0 / N / kRadius / (kPi / Mh);
     // dgd = - mass_div_lon - mass_div_lat with mass_div_lon = 0 at poles
     const T val = T(-0.0) - T(s);
-    for (int i = threadIdx.x; i < N; i += blockDim.x) rdg[i] = val;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) x[i] = val;
     __syncthreads();
   }
   const size_t ro = (size_t)j * N;
-  if (has_du && (info & RI_FLAG_FULL))
-    filter_rescale(md, rdu, iu_in + ro, (const T*)nullptr, ri_keep_full(info), coefs, redT, a.rescale_rtol, tw);
-  if (has_dv && (info & RI_FLAG_HALF))
-    filter_rescale(md, rdv, iv_in + ro, (const T*)nullptr, ri_keep_half(info), coefs, redT, a.rescale_rtol, tw);
-  if (PASS != kSlowPass && (info & RI_FLAG_FULL))
-    filter_rescale(md, rdg, gd_in + ro, md.ghs + ro, ri_keep_full(info), coefs, redT, a.rescale_rtol, tw);
-  const T cj = cf(md, CF_COS, j);
-  const T chj = has_dv ? ch(md, CH_COS, j) : T(0);
+  if (f == F_IU && has_du && (info & RI_FLAG_FULL))
+    filter_rescale(md, x, iu_in + ro, (const T*)nullptr, ri_keep_full(info), coefs, redT, a.rescale_rtol, tw);
+  if (f == F_IV && (info & RI_FLAG_HALF))
+    filter_rescale(md, x, iv_in + ro, (const T*)nullptr, ri_keep_half(info), coefs, redT, a.rescale_rtol, tw);
+  if (f == F_GD && PASS != kSlowPass && (info & RI_FLAG_FULL))
+    filter_rescale(md, x, gd_in + ro, md.ghs + ro, ri_keep_full(info), coefs, redT, a.rescale_rtol, tw);
+  const T w = f == F_IV ? ch(md, CH_COS, j) : cf(md, CF_COS, j);
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     const size_t o = ro + i;
     // du is 0 on pole rows (never assigned by the reference); inner
     // products skip pole-row du (src/types_mod.F90:355).
-    if (has_du)
-      em.put(F_IU, o, rdu[i], cj, em.base_of(F_IU, o), em.prev_of(F_IU, o));
-    else
+    if (f == F_IU && !has_du)
       em.put(F_IU, o, T(0), T(0), em.base_of(F_IU, o), T(0));
-    if (has_dv) em.put(F_IV, o, rdv[i], chj, em.base_of(F_IV, o), em.prev_of(F_IV, o));
-    em.put(F_GD, o, rdg[i], cj, em.base_of(F_GD, o), em.prev_of(F_GD, o));
+    else
+      em.put(f, o, x[i], w, em.base_of(f, o), em.prev_of(f, o));
   }
 }
 
@@ -1070,16 +1066,16 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
     }
 #undef GDC_BULK
   } else {
-    // ---------------- whole-row task: row index j (full row j, half row j)
-    const int j = w.j0;
+    // ---------------- whole-row task: row j (full row j for gd and iap u,
+    // half row j for iap v), field w.field or all three (w.field < 0)
+    const int j = w.j0, f = w.field;
     twiddles_to_shared(md, tw);
-    const int info = md.rowinfo[j];
     const bool has_du = (j >= 1 && j <= M - 2);
     const bool has_dv = (j <= Mh - 1);
     const bool south = (j == 0), north = (j == M - 1);
-    T* rdu = rows;
-    T* rdv = rows + max_n;
-    T* rdg = rows + 2 * max_n;
+    const bool want_u = f < 0 || f == F_IU, want_v = has_dv && (f < 0 || f == F_IV), want_g = f < 0 || f == F_GD;
+    T* xr[3] = {rows + 2 * max_n, rows, rows + max_n};  // by field: gd, iap u, iap v
+    if (f >= 0) xr[f] = rows;
     Acc<double> cap;
     using TR = Tile<T, 1, kRowChunk>;
     for (int c0 = 0; c0 < N; c0 += kRowChunk) {
@@ -1092,8 +1088,9 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
         const int p = TR::pos(1, c + 1);
         const int i = c0 + c;
         const TileView<T, TR> sv{t, p, j};
-        rdu[i] = has_du ? point_du<T, PASS, ADV>(sv, ub_lon, ub_lat) : T(0);
-        rdv[i] = has_dv ? point_dv<T, PASS, ADV>(sv, ub_lon, ub_lat) : T(0);
+        if (want_u) xr[F_IU][i] = has_du ? point_du<T, PASS, ADV>(sv, ub_lon, ub_lat) : T(0);
+        if (want_v) xr[F_IV][i] = point_dv<T, PASS, ADV>(sv, ub_lon, ub_lat);
+        if (!want_g) continue;
         if (south || north) {
           // src/dycore_mod.F90:572-596: sp += (ig(j)+ig(j+1)) iv(j);
           // np -= (ig(j)+ig(j-1)) iv(j-1).  Terms and sum in FP64.
@@ -1103,14 +1100,16 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
             else
               cap.add(((double)t.ig[p] + (double)t.ig[p - TR::SW]) * (double)t.iv[p - TR::SW]);
           }
-          rdg[i] = T(0);
+          xr[F_GD][i] = T(0);
         } else {
-          rdg[i] = point_dgd<T, PASS>(sv);
+          xr[F_GD][i] = point_dgd<T, PASS>(sv);
         }
       }
     }
     __syncthreads();
-    row_tail<T, PASS>(md, a, em, j, rdu, rdv, rdg, cap, coefs, redT, gd_in, iu_in, iv_in, tw);
+    if (want_u) row_tail<T, PASS>(md, a, em, j, F_IU, xr[F_IU], cap, coefs, redT, gd_in, iu_in, iv_in, tw);
+    if (want_v) row_tail<T, PASS>(md, a, em, j, F_IV, xr[F_IV], cap, coefs, redT, gd_in, iu_in, iv_in, tw);
+    if (want_g) row_tail<T, PASS>(md, a, em, j, F_GD, xr[F_GD], cap, coefs, redT, gd_in, iu_in, iv_in, tw);
   }
 
   if (a.do_ip) {
@@ -1467,6 +1466,7 @@ __global__ void __launch_bounds__(kThreads)
   T* tw = redT + 64 + 64 * (int)(sizeof(double) / sizeof(T));  // 2 * max_n twiddles
   __shared__ MemberDev<T> smd;
   const WorkItem w = wl[blockIdx.x];
+  if (w.kind == 1 && w.field > 0) return;  // one block per whole row here (field -1 or F_GD)
   load_member(mems, w.member, &smd);
   const MemberDev<T>& md = smd;
   const int N = md.N, M = md.M, Mh = md.Mh;
@@ -1564,6 +1564,7 @@ __global__ void __launch_bounds__(kThreads)
                          int* uvslot) {
   __shared__ MemberDev<T> smd;
   const WorkItem w = wl[blockIdx.x];
+  if (w.kind == 1 && w.field > 0) return;  // one block per whole row here (field -1 or F_GD)
   load_member(mems, w.member, &smd);
   const MemberDev<T>& md = smd;
   const int N = md.N, Mh = md.Mh;
@@ -1605,6 +1606,7 @@ __global__ void __launch_bounds__(kThreads)
     copy_state_kernel(const MemberDev<T>* __restrict__ mems, const WorkItem* __restrict__ wl, int from, int to) {
   __shared__ MemberDev<T> smd;
   const WorkItem w = wl[blockIdx.x];
+  if (w.kind == 1 && w.field > 0) return;  // one block per whole row here (field -1 or F_GD)
   load_member(mems, w.member, &smd);
   const MemberDev<T>& md = smd;
   const int N = md.N, Mh = md.Mh;

@@ -132,7 +132,9 @@ extern "C" int gdc_tendency_noalloc(const gdc_params* p, int pass, const double*
   const int tile_r = 8, tile_c = 32;
   std::vector<WorkItem> wl;
   for (int j = 0; j < M; ++j)
-    if (rowinfo[j] & RI_SPECIAL) wl.push_back(WorkItem{0, 1, j, 0, 1, N, (int)wl.size(), 0});
+    if (rowinfo[j] & RI_SPECIAL)
+      for (int f : {F_GD, F_IU, F_IV})
+        if (f != F_IV || j < M - 1) wl.push_back(WorkItem{0, 1, j, 0, 1, N, (int)wl.size(), f});
   for (int j = 0; j < M;) {
     if (rowinfo[j] & RI_SPECIAL) {
       ++j;

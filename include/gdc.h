@@ -273,7 +273,7 @@ int gdc_batch_active(gdc_batch* b, int* n_active);
 /* Work layout of the stage kernels: shared-memory tiles of rows x columns
  * (8x32, 8x64, 4x128, 16x64) or warp strips of rows x 30 columns (8x30, 16x30,
  * 32x30, 64x30: one warp marches a 30-column strip down a band of rows);
- * 0,0 picks the default (FP32 16x64, FP64 8x64 tiles).
+ * 0,0 picks the default (FP32 16x64, FP64 8x32 tiles).
  * gdc_batch_autotune times the candidates on the current members and keeps
  * the fastest; the chosen shape is returned. */
 int gdc_batch_set_tile(gdc_batch* b, int tile_rows, int tile_cols);
