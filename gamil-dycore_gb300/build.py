@@ -58,17 +58,17 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     OUT.mkdir(exist_ok=True)
     lib = OUT / "libgdc.so"
     headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [INCLUDE / "gdc.h"]
-    cu = [CSRC / "gdc_kernels_f64.cu", CSRC / "gdc_kernels_f32.cu", CSRC / "gdc_noalloc.cu"]
+    cu = [CSRC / "gdc_kernels_f64.cu", CSRC / "gdc_kernels_f32.cu", CSRC / "gdc_noalloc.cu", CSRC / "gdc_ic.cu"]
     cpp = [CSRC / "gdc_engine.cpp", CSRC / "gdc_host.cpp"]
     if force or _stale(lib, cu + cpp + headers):
         cmds, objs = [], []
         for src in cu:
             obj = OUT / (src.stem + ".o")
             objs.append(obj)
-            # The FP64 unit keeps the reference's rounding: no FMA contraction.
+            # The FP64 units keep the reference's rounding: no FMA contraction.
             # The FP32 unit uses fast single-precision division and square
             # root (fast math affects single precision only).
-            fmad = ["--fmad=false"] if src.stem.endswith(("_f64", "_noalloc")) else ["--use_fast_math"]
+            fmad = ["--fmad=false"] if src.stem.endswith(("_f64", "_noalloc", "_ic")) else ["--use_fast_math"]
             cmds.append([nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", *fmad, "-Xcompiler",
                          "-fPIC,-ffp-contract=off", f"-I{INCLUDE}", "-c", str(src), "-o", str(obj)])
         for src in cpp:

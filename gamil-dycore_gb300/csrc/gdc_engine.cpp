@@ -118,6 +118,8 @@ struct BatchIface {
   virtual int add(int N, int M, double dt, long long nsteps, const int* cutoff, const double* u,
                   const double* v, const double* gd, const double* ghs, int ld, size_t reserve,
                   int* id) = 0;
+  virtual int add_ic(int N, int M, double dt, long long nsteps, const int* cutoff, const gdc_ic_spec& spec,
+                     size_t reserve, int* id) = 0;
   virtual int remove(int id) = 0;
   virtual int step(int n) = 0;
   virtual int sync() = 0;
@@ -175,11 +177,14 @@ class Batch final : public BatchIface {
   }
 
   // ------------------------------------------------------------ members
-  int add(int N, int M, double dt, long long nsteps, const int* cutoff, const double* u,
-          const double* v, const double* gd, const double* ghs, int ld, size_t reserve,
-          int* id) override {
-    if (N < 8 || M < 5 || ld < N + 4 || !(dt > 0) || nsteps < 0 || !u || !v || !gd || !ghs)
-      return fail(GDC_E_CONFIG, "add: invalid grid, time step, length or buffers");
+  // Admission shared by the host and the device initial conditions: checks,
+  // a member slot, device memory (`extra` bytes more must stay free for the
+  // caller's temporaries), the member's tables and its descriptor, all in
+  // device memory; the state fields are left zero.
+  int admit(int N, int M, double dt, long long nsteps, const int* cutoff, size_t reserve, size_t extra,
+            int* out_slot) {
+    if (N < 8 || M < 5 || !(dt > 0) || nsteps < 0)
+      return fail(GDC_E_CONFIG, "add: invalid grid, time step or length");
     if (N % 4 != 0)
       return fail(GDC_E_CONFIG, "add: num_lon must be a multiple of 4 (tile rows are copied 16 bytes at a time)");
     gdc_params mp = P;  // this member's filter rows
@@ -190,13 +195,6 @@ class Batch final : public BatchIface {
       if (c < 0 || 2 * (c + 1) >= N || 2 * (c + 1) > 120)
         return fail(GDC_E_CONFIG, "zonal_tend_filter_cutoff_wavenumber out of range for this grid");
     }
-    // Pole-row u must vanish: u(:,1) and u(:,num_lat) are never updated by
-    // the reference (update_state writes rows 2..num_lat-1 only), and every
-    // reference initial condition sets them to zero.
-    for (int jp : {0, M - 1})
-      for (int i = 0; i < N; ++i)
-        if (u[(size_t)(jp + 2) * ld + i + 2] != 0.0)
-          return fail(GDC_E_CONFIG, "pole-row u must be zero in the initial condition");
     int slot = -1;
     for (int s = 0; s < kSlots; ++s)
       if (!recs[s].used) {
@@ -207,7 +205,7 @@ class Batch final : public BatchIface {
     const Layout L = make_layout<T>(mp, N, M);
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
-    if (free_b < L.total + reserve) return fail(GDC_E_OOM, "add: not enough free device memory");
+    if (free_b < L.total + reserve + extra) return fail(GDC_E_OOM, "add: not enough free device memory");
     MemberRec& r = recs[slot];
     r = MemberRec();
     cudaError_t e = cudaMalloc(&r.dmem, L.total);
@@ -271,29 +269,6 @@ class Batch final : public BatchIface {
       dco[M + j] = co.full_cos[j];
     }
     for (int j = 0; j < Mh; ++j) dco[2 * M + j] = co.half_cos[j];
-    // iap_transform of the initial condition (src/types_mod.F90:399-426) in
-    // FP64 on the host, exactly as the reference evaluates it.
-    const size_t full = (size_t)M * N, half = (size_t)Mh * N;
-    std::vector<double> hg(full), hu(full), hv(half), hghs(full);
-    auto at = [&](const double* f, int i, int j) { return f[(size_t)(j + 2) * ld + (i + 2)]; };
-    std::vector<double> ig(full);
-    for (int j = 0; j < M; ++j)
-      for (int i = 0; i < N; ++i) {
-        hg[(size_t)j * N + i] = at(gd, i, j);
-        hghs[(size_t)j * N + i] = at(ghs, i, j);
-        ig[(size_t)j * N + i] = std::sqrt(at(gd, i, j));
-      }
-    for (int j = 0; j < M; ++j)
-      for (int i = 0; i < N; ++i) {
-        const int ip = (i + 1) % N;
-        hu[(size_t)j * N + i] = 0.5 * (ig[(size_t)j * N + i] + ig[(size_t)j * N + ip]) * at(u, i, j);
-      }
-    for (int j = 0; j < Mh; ++j)
-      for (int i = 0; i < N; ++i)
-        hv[(size_t)j * N + i] = 0.5 * (ig[(size_t)j * N + i] + ig[(size_t)(j + 1) * N + i]) * at(v, i, j);
-    r.ic_ld = ld;
-    r.ic_u.assign(u, u + (size_t)ld * (M + 4));
-    r.ic_v.assign(v, v + (size_t)ld * (Mh + 4));
     // Descriptor.
     MemberDev<T>& d = hdesc[slot];
     std::memset(&d, 0, sizeof(d));
@@ -328,7 +303,77 @@ class Batch final : public BatchIface {
     if (e == cudaSuccess) e = cudaMemcpy(base + L.twid, twid.data(), twid.size() * sizeof(T), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(base + L.rowinfo, r.rowinfo.data(), M * sizeof(int), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(base + L.dcoef, dco.data(), dco.size() * sizeof(double), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = upload_field(d.ghs, nullptr, hghs);
+    if (e == cudaSuccess) e = cudaMemcpy(d_mem + slot, &d, sizeof(d), cudaMemcpyHostToDevice);
+    const long long minus1 = -1, zero = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(d_nan + slot, &minus1, sizeof(minus1), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_steps + slot, &zero, sizeof(zero), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      release(slot);
+      return fail(GDC_E_CUDA, cuda_msg("add: upload", e));
+    }
+    *out_slot = slot;
+    return GDC_OK;
+  }
+
+  // A slot that admit() gave out and whose state could not be written.
+  void release(int slot) {
+    cudaFree(recs[slot].dmem);
+    recs[slot] = MemberRec();
+  }
+
+  // Admission's end: the member joins the work lists and gets the
+  // diagnostics of its initial state (diag_run, src/dycore_mod.F90:125).
+  int finish(int slot, int* id) {
+    MemberRec& r = recs[slot];
+    r.active = r.nsteps > 0;
+    r.finished = r.nsteps == 0;
+    dirty = true;
+    if (int rc = initial_diag(slot)) return rc;
+    *id = slot;
+    return GDC_OK;
+  }
+
+  int add(int N, int M, double dt, long long nsteps, const int* cutoff, const double* u,
+          const double* v, const double* gd, const double* ghs, int ld, size_t reserve,
+          int* id) override {
+    if (ld < N + 4 || !u || !v || !gd || !ghs || N < 8 || M < 5)
+      return fail(GDC_E_CONFIG, "add: invalid grid, leading dimension or buffers");
+    // Pole-row u must vanish: u(:,1) and u(:,num_lat) are never updated by
+    // the reference (update_state writes rows 2..num_lat-1 only), and every
+    // reference initial condition sets them to zero.
+    for (int jp : {0, M - 1})
+      for (int i = 0; i < N; ++i)
+        if (u[(size_t)(jp + 2) * ld + i + 2] != 0.0)
+          return fail(GDC_E_CONFIG, "pole-row u must be zero in the initial condition");
+    int slot = -1;
+    if (int rc = admit(N, M, dt, nsteps, cutoff, reserve, 0, &slot)) return rc;
+    MemberRec& r = recs[slot];
+    const MemberDev<T>& d = hdesc[slot];
+    const int Mh = M - 1;
+    // iap_transform of the initial condition (src/types_mod.F90:399-426) in
+    // FP64 on the host, exactly as the reference evaluates it.
+    const size_t full = (size_t)M * N, half = (size_t)Mh * N;
+    std::vector<double> hg(full), hu(full), hv(half), hghs(full);
+    auto at = [&](const double* f, int i, int j) { return f[(size_t)(j + 2) * ld + (i + 2)]; };
+    std::vector<double> ig(full);
+    for (int j = 0; j < M; ++j)
+      for (int i = 0; i < N; ++i) {
+        hg[(size_t)j * N + i] = at(gd, i, j);
+        hghs[(size_t)j * N + i] = at(ghs, i, j);
+        ig[(size_t)j * N + i] = std::sqrt(at(gd, i, j));
+      }
+    for (int j = 0; j < M; ++j)
+      for (int i = 0; i < N; ++i) {
+        const int ip = (i + 1) % N;
+        hu[(size_t)j * N + i] = 0.5 * (ig[(size_t)j * N + i] + ig[(size_t)j * N + ip]) * at(u, i, j);
+      }
+    for (int j = 0; j < Mh; ++j)
+      for (int i = 0; i < N; ++i)
+        hv[(size_t)j * N + i] = 0.5 * (ig[(size_t)j * N + i] + ig[(size_t)(j + 1) * N + i]) * at(v, i, j);
+    r.ic_ld = ld;
+    r.ic_u.assign(u, u + (size_t)ld * (M + 4));
+    r.ic_v.assign(v, v + (size_t)ld * (Mh + 4));
+    cudaError_t e = upload_field(d.ghs, nullptr, hghs);
     const int lvl = old_;
     if (e == cudaSuccess) e = upload_field(d.st[lvl][F_GD], d.lo[lvl][F_GD], hg);
     if (e == cudaSuccess) e = upload_field(d.st[lvl][F_IU], d.lo[lvl][F_IU], hu);
@@ -345,22 +390,72 @@ class Batch final : public BatchIface {
       if (e == cudaSuccess) e = upload_field(d.given_v, nullptr, gv);
       if (e == cudaSuccess) e = cudaMemcpy(d_uvslot + slot, &lvl, sizeof(int), cudaMemcpyHostToDevice);
     }
-    if (e == cudaSuccess) e = cudaMemcpy(d_mem + slot, &d, sizeof(d), cudaMemcpyHostToDevice);
-    const long long minus1 = -1, zero = 0;
-    if (e == cudaSuccess) e = cudaMemcpy(d_nan + slot, &minus1, sizeof(minus1), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(d_steps + slot, &zero, sizeof(zero), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
-      cudaFree(r.dmem);
-      r = MemberRec();
+      release(slot);
       return fail(GDC_E_CUDA, cuda_msg("add: upload", e));
     }
-    r.active = nsteps > 0;
-    r.finished = nsteps == 0;
-    dirty = true;
-    // diag_run of the initial state (src/dycore_mod.F90:125).
-    if (int rc = initial_diag(slot)) return rc;
-    *id = slot;
-    return GDC_OK;
+    return finish(slot, id);
+  }
+
+  // A member whose initial condition is generated in device memory
+  // (gdc_batch_add_ic): the host sends only the mesh coordinates and, for
+  // the seeded state, its random draws; the fields, their IAP transform and
+  // the given u, v are computed on the device.
+  int add_ic(int N, int M, double dt, long long nsteps, const int* cutoff, const gdc_ic_spec& spec,
+             size_t reserve, int* id) override {
+    if (spec.kind < GDC_IC_ROSSBY_HAURWITZ || spec.kind > GDC_IC_SEEDED)
+      return fail(GDC_E_CONFIG, "add_ic: unknown initial condition kind");
+    if (spec.kind == GDC_IC_SEEDED &&
+        (spec.lmax < 0 || spec.lmax > 64 || spec.n_mountains < 0 || spec.n_mountains > 4096))
+      return fail(GDC_E_CONFIG, "add_ic: lmax must be in 0..64 and n_mountains in 0..4096");
+    if (!(spec.noise_sigma >= 0)) return fail(GDC_E_CONFIG, "add_ic: noise_sigma must be >= 0");
+    if (N < 8 || M < 5) return fail(GDC_E_CONFIG, "add_ic: invalid grid");
+    const Mesh mesh = make_mesh(N, M);
+    const int Mh = M - 1;
+    std::vector<double> tables;
+    auto append = [&](const std::vector<double>& x, size_t n) { tables.insert(tables.end(), x.begin(), x.begin() + n); };
+    append(mesh.full_lat, M);
+    append(mesh.half_lat, Mh);
+    append(mesh.full_lon, N);
+    append(mesh.half_lon, N);
+    append(mesh.full_cos, M);
+    append(mesh.half_cos, Mh);
+    append(mesh.full_sin, M);
+    append(mesh.half_sin, Mh);
+    if (spec.kind == GDC_IC_SEEDED) {
+      std::vector<double> clat, clon, ag, bg, ap, bp;
+      seeded_draws(spec.seed, spec.lmax, spec.n_mountains, clat, clon, ag, bg, ap, bp);
+      for (const auto* x : {&clat, &clon, &ag, &bg, &ap, &bp}) append(*x, x->size());
+    }
+    const size_t n = (size_t)M * N;
+    // u, v, gd, ghs, the generator's scratch, the tables.
+    const size_t tmp_words = 4 * n + 2 * n + 2 + tables.size();
+    int slot = -1;
+    if (int rc = admit(N, M, dt, nsteps, cutoff, reserve, tmp_words * sizeof(double), &slot)) return rc;
+    double* tmp = nullptr;
+    cudaError_t e = cudaMalloc(&tmp, tmp_words * sizeof(double));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      release(slot);
+      return fail(GDC_E_OOM, cuda_msg("add_ic: cudaMalloc", e));
+    }
+    double *du = tmp, *dv = du + n, *dg = dv + n, *dh = dg + n, *scratch = dh + n, *dt_tab = scratch + 2 * n + 2;
+    const int lvl = old_;
+    e = cudaMemcpyAsync(dt_tab, tables.data(), tables.size() * sizeof(double), cudaMemcpyHostToDevice, stream);
+    int rc = e == cudaSuccess ? ic_generate(spec, N, M, dt_tab, scratch, du, dv, dg, dh, stream) : GDC_E_CUDA;
+    if (rc == GDC_OK) rc = launch_ic_iap<T>(d_mem, slot, lvl, N, M, du, dv, dg, dh, stream);
+    if (rc == GDC_OK)
+      rc = cudaMemcpyAsync(d_uvslot + slot, &lvl, sizeof(int), cudaMemcpyHostToDevice, stream) == cudaSuccess
+               ? GDC_OK
+               : GDC_E_CUDA;
+    e = cudaStreamSynchronize(stream);
+    cudaFree(tmp);
+    if (rc != GDC_OK || e != cudaSuccess) {
+      if (e == cudaSuccess) e = cudaGetLastError();
+      release(slot);
+      return fail(GDC_E_CUDA, cuda_msg("add_ic: generate", e));
+    }
+    return finish(slot, id);
   }
 
   int checkpoint(int id, const char* path) override {
@@ -677,7 +772,7 @@ class Batch final : public BatchIface {
     put(ig, M, [&](int i, int j) { return sg[(size_t)j * N + i]; });
     int uvs = -1;
     cudaMemcpy(&uvs, d_uvslot + id, sizeof(int), cudaMemcpyDeviceToHost);
-    if (r.steps_done == 0 && std::is_same<T, double>::value) {
+    if (r.steps_done == 0 && std::is_same<T, double>::value && !r.ic_u.empty()) {
       // state(old) still holds the initial condition's own u and v.
       auto copy_ic = [&](double* f, const std::vector<double>& src, int rows) {
         if (!f) return;
@@ -1580,6 +1675,11 @@ int gdc_batch_add(gdc_batch* b, int num_lon, int num_lat, double time_step_size,
   if (!b || !member_id) return GDC_E_CONFIG;
   return b->impl->add(num_lon, num_lat, time_step_size, nsteps, cutoff, u, v, gd, ghs, ld,
                       reserve_bytes, member_id);
+}
+int gdc_batch_add_ic(gdc_batch* b, int num_lon, int num_lat, double time_step_size, long long nsteps,
+                     const int* cutoff, const gdc_ic_spec* spec, size_t reserve_bytes, int* member_id) {
+  if (!b || !spec || !member_id) return GDC_E_CONFIG;
+  return b->impl->add_ic(num_lon, num_lat, time_step_size, nsteps, cutoff, *spec, reserve_bytes, member_id);
 }
 int gdc_batch_remove(gdc_batch* b, int id) { return b ? b->impl->remove(id) : GDC_E_CONFIG; }
 int gdc_batch_step(gdc_batch* b, int nsteps) { return b ? b->impl->step(nsteps) : GDC_E_CONFIG; }

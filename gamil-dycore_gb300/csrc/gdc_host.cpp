@@ -582,6 +582,27 @@ extern "C" int gdc_ic_mountain_zonal_flow(int N, int M, double* u, double* v, do
   return GDC_OK;
 }
 
+namespace gdc {
+// The random draws of gdc_ic_seeded, in its order (mountain centres, then
+// the gd and the streamfunction harmonics), for the device generator.
+void seeded_draws(unsigned long long seed, int lmax, int n_mountains, std::vector<double>& clat,
+                  std::vector<double>& clon, std::vector<double>& ag, std::vector<double>& bg,
+                  std::vector<double>& ap, std::vector<double>& bp) {
+  Rng rng(seed);
+  clat.assign(n_mountains, 0.0);
+  clon.assign(n_mountains, 0.0);
+  for (int k = 0; k < n_mountains; ++k) {
+    clon[k] = 2 * kPi * rng.uniform();
+    clat[k] = std::asin(2 * rng.uniform() - 1);
+  }
+  Harmonics hg(lmax, rng), hp(lmax, rng);
+  ag = hg.a;
+  bg = hg.b;
+  ap = hp.a;
+  bp = hp.b;
+}
+}  // namespace gdc
+
 extern "C" int gdc_ic_seeded(int N, int M, unsigned long long seed, int lmax, double gd0,
                              double gd_rms, double psi_rms, double u0, int n_mountains,
                              double mountain_height, double mountain_radius_deg, double* u,
@@ -652,6 +673,18 @@ extern "C" int gdc_ic_seeded(int N, int M, unsigned long long seed, int lmax, do
   fill_lon_halo(u, ld, N, M); fill_lon_halo(v, ld, N, Mh);
   fill_lon_halo(gd, ld, N, M); fill_lon_halo(ghs, ld, N, M);
   return GDC_OK;
+}
+
+extern "C" void gdc_ic_spec_default(gdc_ic_spec* spec, int kind) {
+  if (!spec) return;
+  std::memset(spec, 0, sizeof(*spec));
+  spec->kind = kind;
+  spec->lmax = 6;
+  spec->gd0 = 8000.0 * kG;
+  spec->gd_rms = 100.0 * kG;
+  spec->psi_rms = 1.0e7;
+  spec->mountain_height = 2000.0;
+  spec->mountain_radius_deg = 20.0;
 }
 
 extern "C" int gdc_ic_add_noise(int N, int M, unsigned long long seed, double sigma, double* gd,

@@ -37,6 +37,18 @@ Coef make_coef(const Mesh& m);
 void make_filter_rows(const Mesh& m, const gdc_params& p, std::vector<int>& flag_full,
                       std::vector<int>& keep_full, std::vector<int>& flag_half,
                       std::vector<int>& keep_half);
+void seeded_draws(unsigned long long seed, int lmax, int n_mountains, std::vector<double>& clat,
+                  std::vector<double>& clon, std::vector<double>& ag, std::vector<double>& bg,
+                  std::vector<double>& ap, std::vector<double>& bp);
+
+// Device initial conditions (gdc_ic.cu): FP64 fields, interior only, lon
+// fastest: u, gd, ghs num_lat rows, v num_lat - 1.  `tables` holds the mesh
+// (full_lat, half_lat, full_lon, half_lon, full_cos, half_cos, full_sin,
+// half_sin: M, Mh, N, N, M, Mh, M, Mh values) followed, for the seeded state,
+// by the mountain centres (lat, lon) and the harmonic coefficients (gd a, b,
+// streamfunction a, b; (lmax+1)^2 each); `scratch` 2 M N + 2 doubles.
+int ic_generate(const gdc_ic_spec& spec, int N, int M, const double* tables, double* scratch, double* u,
+                double* v, double* gd, double* ghs, void* stream);
 
 // ------------------------------------------------------------ device layout
 // Passes of space_operators (src/dycore_mod.F90:34-36).
@@ -269,6 +281,11 @@ int launch_stage_strips(const MemberDev<T>* mem, const WorkItem* strips, int nst
                         void* stream);
 // History output of member `slot` at level `lvl` into device FP64 buffers
 // (num_lat x num_lon each; vor num_lat - 1 rows).
+// iap_transform of a device initial condition into member `slot`'s level
+// `lvl`, its given u, v and ghs (src/types_mod.F90:399-426).
+template <typename T>
+int launch_ic_iap(const MemberDev<T>* mem, int slot, int lvl, int N, int M, const double* u, const double* v,
+                  const double* gd, const double* ghs, void* stream);
 template <typename T>
 int launch_history(const MemberDev<T>* mem, int slot, int lvl, int given, int num_lat, double* ua, double* va,
                    double* gh, double* div, double* vor, void* stream);

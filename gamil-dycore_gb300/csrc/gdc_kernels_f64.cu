@@ -15,6 +15,8 @@ template int launch_stage<double>(const MemberDev<double>*, const WorkItem*, int
 template int launch_stage_strips<double>(const MemberDev<double>*, const WorkItem*, int, int, const StageArgs&, void*);
 template int launch_history<double>(const MemberDev<double>*, int, int, int, int, double*, double*, double*, double*,
                                    double*, void*);
+template int launch_ic_iap<double>(const MemberDev<double>*, int, int, int, int, const double*, const double*,
+                                 const double*, const double*, void*);
 template int launch_final<double>(const MemberDev<double>*, const FlatItem*, int, const FinalArgs&, void*);
 template int launch_diag<double>(const MemberDev<double>*, const FlatItem*, int, const int*, int, const DiagArgs&, void*);
 template int launch_beta<double>(const MemberDev<double>*, const int*, int, const double*, double*, int, int, void*);

@@ -64,6 +64,29 @@ class Params(ctypes.Structure):
     ]
 
 
+IC_ROSSBY_HAURWITZ, IC_STEADY_GEOSTROPHIC, IC_MOUNTAIN_ZONAL_FLOW, IC_SEEDED = 0, 1, 2, 3
+
+
+class ICSpec(ctypes.Structure):
+    """Mirror of ``gdc_ic_spec``: an initial condition generated on the device."""
+
+    _fields_ = [
+        ("kind", ctypes.c_int),
+        ("lmax", ctypes.c_int),
+        ("seed", ctypes.c_ulonglong),
+        ("gd0", ctypes.c_double),
+        ("gd_rms", ctypes.c_double),
+        ("psi_rms", ctypes.c_double),
+        ("u0", ctypes.c_double),
+        ("n_mountains", ctypes.c_int),
+        ("reserved", ctypes.c_int),
+        ("mountain_height", ctypes.c_double),
+        ("mountain_radius_deg", ctypes.c_double),
+        ("noise_seed", ctypes.c_ulonglong),
+        ("noise_sigma", ctypes.c_double),
+    ]
+
+
 _lib = None
 _P = ctypes.POINTER(ctypes.c_double)
 
@@ -116,6 +139,9 @@ def lib() -> ctypes.CDLL:
                                                    ctypes.POINTER(ctypes.c_size_t)]),
             "gdc_batch_add": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_longlong,
                                              ip, dp, dp, dp, dp, ctypes.c_int, ctypes.c_size_t, ip]),
+            "gdc_ic_spec_default": (None, [ctypes.POINTER(ICSpec), ctypes.c_int]),
+            "gdc_batch_add_ic": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_longlong,
+                                                ip, ctypes.POINTER(ICSpec), ctypes.c_size_t, ip]),
             "gdc_batch_remove": (ctypes.c_int, [vp, ctypes.c_int]),
             "gdc_batch_step": (ctypes.c_int, [vp, ctypes.c_int]),
             "gdc_batch_sync": (ctypes.c_int, [vp]),
@@ -150,6 +176,26 @@ def _ptr(a: np.ndarray | None):
         return None
     assert a.dtype == np.float64 and a.flags.c_contiguous
     return a.ctypes.data_as(_P)
+
+
+def ic_spec(kind: int, **kw) -> ICSpec:
+    """gdc_ic_spec_default(kind) with fields overridden by keyword."""
+    spec = ICSpec()
+    lib().gdc_ic_spec_default(ctypes.byref(spec), kind)
+    for k, v in kw.items():
+        if not hasattr(spec, k):
+            raise AttributeError(f"gdc_ic_spec has no field {k}")
+        setattr(spec, k, v)
+    return spec
+
+
+def _cutoff_array(cutoff):
+    if cutoff is None:
+        return None
+    cut = (ctypes.c_int * 20)(*([0] * 20))
+    for q, c in enumerate(cutoff):
+        cut[q] = int(c)
+    return cut
 
 
 def padded(rows: int, num_lon: int) -> np.ndarray:
@@ -364,13 +410,19 @@ class Batch:
         """Admit a member; `cutoff` overrides the scheme's filter cutoffs."""
         mid = ctypes.c_int()
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (u, v, gd, ghs)]
-        cut = None
-        if cutoff is not None:
-            cut = (ctypes.c_int * 20)(*([0] * 20))
-            for q, c in enumerate(cutoff):
-                cut[q] = int(c)
-        rc = lib().gdc_batch_add(self.b, N, M, dt, nsteps, cut, *map(_ptr, arrs), N + 4, reserve_bytes,
-                                 ctypes.byref(mid))
+        rc = lib().gdc_batch_add(self.b, N, M, dt, nsteps, _cutoff_array(cutoff), *map(_ptr, arrs), N + 4,
+                                 reserve_bytes, ctypes.byref(mid))
+        self._check(rc)
+        self.grids[mid.value] = (N, M)
+        return mid.value
+
+    def add_ic(self, N: int, M: int, dt: float, nsteps: int, spec: ICSpec, reserve_bytes: int = 0,
+               cutoff=None) -> int:
+        """Admit a member whose initial condition (`spec`, see ``ic_spec``)
+        is generated in device memory."""
+        mid = ctypes.c_int()
+        rc = lib().gdc_batch_add_ic(self.b, N, M, dt, nsteps, _cutoff_array(cutoff), ctypes.byref(spec),
+                                    reserve_bytes, ctypes.byref(mid))
         self._check(rc)
         self.grids[mid.value] = (N, M)
         return mid.value

@@ -22,7 +22,8 @@ import time
 
 import numpy as np
 
-from . import E_OOM, FP32, G, SPLIT_CSP2, Batch, GdcError, default_params, ic_add_noise, ic_seeded
+from . import (E_OOM, FP32, G, IC_SEEDED, SPLIT_CSP2, Batch, GdcError, ICSpec, default_params, ic_add_noise,
+               ic_seeded, ic_spec)
 
 # grid (degrees of resolution) -> num_lon, num_lat, time step (240 s per
 # degree), steps per model day, filter cutoffs of the near-pole rows
@@ -83,14 +84,20 @@ def serving_scheme(precision: int = FP32):
 
 class InitialStates:
     """Seeded initial states: the degree 1..6 harmonic state of each grid
-    (built once per grid) plus N(0, 1 m) noise on gd seeded per request."""
+    plus N(0, 1 m) noise on gd seeded per request.  With `device` (the
+    default) the state is generated in device memory at admission
+    (``gdc_batch_add_ic``); otherwise the host builds it (the base state
+    once per grid) and uploads it."""
 
-    def __init__(self, seed: int = 0, noise_m: float = 1.0):
+    def __init__(self, seed: int = 0, noise_m: float = 1.0, device: bool = True):
         self.seed = seed
         self.noise = noise_m * G
+        self.device = device
         self.base = {}
 
     def __call__(self, req: Request):
+        if self.device:
+            return ic_spec(IC_SEEDED, seed=self.seed, noise_seed=1000 + req.rid, noise_sigma=self.noise)
         N, M = GRIDS[req.grid][:2]
         if req.grid not in self.base:
             self.base[req.grid] = ic_seeded(N, M, seed=self.seed)
@@ -142,8 +149,12 @@ class Server:
             while waiting and len(running) < self.max_members:
                 r = waiting[0]
                 N, M, dt, _, cut = GRIDS[r.grid]
+                ic = self.ics(r)
                 try:
-                    mid = self.batch.add(N, M, dt, r.nsteps, *self.ics(r), reserve_bytes=self.reserve, cutoff=cut)
+                    if isinstance(ic, ICSpec):
+                        mid = self.batch.add_ic(N, M, dt, r.nsteps, ic, reserve_bytes=self.reserve, cutoff=cut)
+                    else:
+                        mid = self.batch.add(N, M, dt, r.nsteps, *ic, reserve_bytes=self.reserve, cutoff=cut)
                 except GdcError as e:
                     if e.code == E_OOM and running:
                         break  # wait for completions to free memory

@@ -240,6 +240,35 @@ int gdc_batch_add(gdc_batch* b, int num_lon, int num_lat,
                   const double* u, const double* v, const double* gd,
                   const double* ghs, int ld, size_t reserve_bytes,
                   int* member_id);
+/* Initial conditions generated on the device, for gdc_batch_add_ic: the
+ * same states as the gdc_ic_* functions, without building and uploading host
+ * arrays (admission of large grids costs milliseconds of host time
+ * otherwise).  Parameters of the seeded state as gdc_ic_seeded; a noise
+ * sigma > 0 adds gdc_ic_add_noise's N(0, sigma) white noise (noise_seed). */
+enum {
+  GDC_IC_ROSSBY_HAURWITZ = 0,
+  GDC_IC_STEADY_GEOSTROPHIC = 1,
+  GDC_IC_MOUNTAIN_ZONAL_FLOW = 2,
+  GDC_IC_SEEDED = 3
+};
+typedef struct gdc_ic_spec {
+  int kind;
+  int lmax;
+  unsigned long long seed;
+  double gd0, gd_rms, psi_rms, u0;
+  int n_mountains;
+  int reserved;
+  double mountain_height, mountain_radius_deg;
+  unsigned long long noise_seed;
+  double noise_sigma;
+} gdc_ic_spec;
+/* Defaults of `kind` (seeded: the degree 1..6 state of gdc_ic_seeded's
+ * documentation, seed 0, no mountains, no noise). */
+void gdc_ic_spec_default(gdc_ic_spec* spec, int kind);
+/* gdc_batch_add with the initial condition of `spec` generated in device
+ * memory (FP64, then iap_transform into the member's precision). */
+int gdc_batch_add_ic(gdc_batch* b, int num_lon, int num_lat, double time_step_size, long long nsteps,
+                     const int* cutoff, const gdc_ic_spec* spec, size_t reserve_bytes, int* member_id);
 /* Release a member's device memory (finished or evicted). */
 int gdc_batch_remove(gdc_batch* b, int member_id);
 /* Advance every active, unfinished member by `nsteps` model steps (members

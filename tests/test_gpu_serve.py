@@ -13,7 +13,11 @@ pytestmark = pytest.mark.gpu
 def solo(req, ics):
     N, M, dt, _, cut = serve.GRIDS[req.grid]
     b = gdc.Batch(serve.serving_scheme(gdc.FP32))
-    mid = b.add(N, M, dt, req.nsteps, *ics(req), cutoff=cut)
+    ic = ics(req)
+    if isinstance(ic, gdc.ICSpec):
+        mid = b.add_ic(N, M, dt, req.nsteps, ic, cutoff=cut)
+    else:
+        mid = b.add(N, M, dt, req.nsteps, *ic, cutoff=cut)
     b.step(req.nsteps)
     b.sync()
     out = b.get_state(mid)
@@ -21,11 +25,12 @@ def solo(req, ics):
     return out
 
 
-def test_served_results_equal_solo_runs(native):
+@pytest.mark.parametrize("device_ic", [True, False])
+def test_served_results_equal_solo_runs(native, device_ic):
     rng = np.random.default_rng(5)
     reqs = [serve.Request(rid=k, grid=int(rng.choice([180, 360])), nsteps=int(rng.integers(3, 25)),
-                          arrival=0.02 * k) for k in range(10)]
-    ics = serve.InitialStates(seed=0)
+                          arrival=0.001 * k) for k in range(10)]
+    ics = serve.InitialStates(seed=0, device=device_ic)
     srv = serve.Server(steps_per_tick=3, initial_states=ics)
     stats = srv.run(reqs, keep_results=True)
     srv.close()
