@@ -403,7 +403,7 @@ class Batch final : public BatchIface {
   // the given u, v are computed on the device.
   int add_ic(int N, int M, double dt, long long nsteps, const int* cutoff, const gdc_ic_spec& spec,
              size_t reserve, int* id) override {
-    if (spec.kind < GDC_IC_ROSSBY_HAURWITZ || spec.kind > GDC_IC_SEEDED)
+    if (spec.kind < GDC_IC_ROSSBY_HAURWITZ || spec.kind > GDC_IC_SHALLOW_WATER_WAVES)
       return fail(GDC_E_CONFIG, "add_ic: unknown initial condition kind");
     if (spec.kind == GDC_IC_SEEDED &&
         (spec.lmax < 0 || spec.lmax > 64 || spec.n_mountains < 0 || spec.n_mountains > 4096))
@@ -422,6 +422,14 @@ class Batch final : public BatchIface {
     append(mesh.half_cos, Mh);
     append(mesh.full_sin, M);
     append(mesh.half_sin, Mh);
+    if (spec.kind == GDC_IC_ROSSBY_HAURWITZ || spec.kind == GDC_IC_SHALLOW_WATER_WAVES) {
+      std::vector<double> t;
+      if (spec.kind == GDC_IC_ROSSBY_HAURWITZ)
+        rh_tables(mesh, t);
+      else
+        sw_waves_tables(mesh, t);
+      append(t, t.size());
+    }
     if (spec.kind == GDC_IC_SEEDED) {
       std::vector<double> clat, clon, ag, bg, ap, bp;
       seeded_draws(spec.seed, spec.lmax, spec.n_mountains, clat, clon, ag, bg, ap, bp);

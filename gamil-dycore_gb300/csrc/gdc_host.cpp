@@ -5,7 +5,9 @@
 #include "gdc_internal.h"
 
 #include <cctype>
+#include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -485,45 +487,51 @@ struct Harmonics {
 
 }  // namespace
 
-// src/test_cases/barotropic/rossby_haurwitz_wave_test_mod.F90:33-85
+namespace gdc {
+void rh_tables(const Mesh& m, std::vector<double>& t) {
+  const int N = m.N, M = m.M, Mh = m.Mh;
+  const double R = 4.0, omg = 7.848e-6;
+  t.assign(rh_table_words(N, M), 0.0);
+  for (int j = 0; j < M; ++j) {
+    const double cl = m.full_cos[j], sl = m.full_sin[j];
+    t[j] = cl;
+    t[M + j] = R * std::pow(cl, R - 1) * (sl * sl);
+    t[2 * M + j] = std::pow(cl, R + 1);
+    t[4 * M + j] = 0.5 * omg * (2 * kOmega + omg) * (cl * cl) +
+                   0.25 * omg * omg *
+                       ((R + 1) * std::pow(cl, 2 * R + 2) + (2 * R * R - R - 2) * std::pow(cl, 2 * R) -
+                        2 * R * R * std::pow(cl, 2 * R - 2));
+    t[5 * M + j] = 2 * (kOmega + omg) * omg * std::pow(cl, R) *
+                   (R * R + 2 * R + 2 - (R + 1) * (R + 1) * (cl * cl)) / (R + 1) / (R + 2);
+    t[6 * M + j] = 0.25 * omg * omg * std::pow(cl, 2 * R) * ((R + 1) * (cl * cl) - R - 2);
+  }
+  for (int j = 0; j < Mh; ++j) t[3 * M + j] = R * std::pow(m.half_cos[j], R - 1) * m.half_sin[j];
+  double* col = t.data() + 7 * (size_t)M;
+  for (int i = 0; i < N; ++i) {
+    col[i] = std::cos(R * m.half_lon[i]);
+    col[N + i] = std::sin(R * m.full_lon[i]);
+    col[2 * N + i] = std::cos(R * m.full_lon[i]);
+    col[3 * N + i] = std::cos(2 * R * m.full_lon[i]);
+  }
+}
+}  // namespace gdc
+
+// src/test_cases/barotropic/rossby_haurwitz_wave_test_mod.F90:33-85: the
+// factor tables of rh_tables and their products (rh_u, rh_v, rh_gd), which
+// evaluate the reference's expressions in its order.
 extern "C" int gdc_ic_rossby_haurwitz(int N, int M, double* u, double* v, double* gd,
                                       double* ghs, int ld) {
   if (!check_grid(N, M, ld) || !u || !v || !gd || !ghs) return GDC_E_CONFIG;
   const gdc::Mesh m = gdc::make_mesh(N, M);
-  const double R = 4.0, omg = 7.848e-6, gd0 = 8.0e3 * kG;
+  std::vector<double> t;
+  gdc::rh_tables(m, t);
   zero_field(u, ld, M); zero_field(v, ld, M - 1); zero_field(gd, ld, M); zero_field(ghs, ld, M);
-  for (int j = 0; j < M; ++j) {
-    const double cl = m.full_cos[j], sl = m.full_sin[j];
+  for (int j = 0; j < M; ++j)
     for (int i = 0; i < N; ++i) {
-      const double lon = m.half_lon[i];
-      const double a = cl;
-      const double b = R * std::pow(cl, R - 1) * (sl * sl) * std::cos(R * lon);
-      const double c = std::pow(cl, R + 1) * std::cos(R * lon);
-      P(u, ld, i, j) = kRadius * omg * (a + b - c);
+      P(u, ld, i, j) = gdc::rh_u(t.data(), N, M, i, j);
+      P(gd, ld, i, j) = gdc::rh_gd(t.data(), N, M, i, j);
+      if (j < M - 1) P(v, ld, i, j) = gdc::rh_v(t.data(), N, M, i, j);
     }
-  }
-  for (int j = 0; j < M - 1; ++j) {
-    const double cl = m.half_cos[j], sl = m.half_sin[j];
-    for (int i = 0; i < N; ++i) {
-      const double lon = m.full_lon[i];
-      const double a = R * std::pow(cl, R - 1) * sl * std::sin(R * lon);
-      P(v, ld, i, j) = -kRadius * omg * a;
-    }
-  }
-  for (int j = 0; j < M; ++j) {
-    const double cl = m.full_cos[j];
-    const double a = 0.5 * omg * (2 * kOmega + omg) * (cl * cl) +
-                     0.25 * omg * omg *
-                         ((R + 1) * std::pow(cl, 2 * R + 2) + (2 * R * R - R - 2) * std::pow(cl, 2 * R) -
-                          2 * R * R * std::pow(cl, 2 * R - 2));
-    const double b = 2 * (kOmega + omg) * omg * std::pow(cl, R) *
-                     (R * R + 2 * R + 2 - (R + 1) * (R + 1) * (cl * cl)) / (R + 1) / (R + 2);
-    const double c = 0.25 * omg * omg * std::pow(cl, 2 * R) * ((R + 1) * (cl * cl) - R - 2);
-    for (int i = 0; i < N; ++i) {
-      const double lon = m.full_lon[i];
-      P(gd, ld, i, j) = gd0 + kRadius * kRadius * (a + b * std::cos(R * lon) + c * std::cos(2 * R * lon));
-    }
-  }
   fill_lon_halo(u, ld, N, M); fill_lon_halo(v, ld, N, M - 1); fill_lon_halo(gd, ld, N, M);
   return GDC_OK;
 }
@@ -581,6 +589,100 @@ extern "C" int gdc_ic_mountain_zonal_flow(int N, int M, double* u, double* v, do
   fill_lon_halo(u, ld, N, M); fill_lon_halo(v, ld, N, M - 1); fill_lon_halo(gd, ld, N, M);
   return GDC_OK;
 }
+
+namespace gdc {
+namespace {
+// Parameters of src/test_cases/barotropic/shallow_water_waves_test_mod.F90:
+// 73-87 (the module's own Earth constants; its sigma and a3..a5 are
+// compile-time constants there, rounded as double arithmetic).
+constexpr double kSwOmega = 7.29212e-5, kSwG = 9.80616, kSwA = 6371220.0, kSwH0 = 5.0e3;
+constexpr double kSwPi = 3.14159265358979323;
+constexpr int kSwN = 5, kSwK = 10;
+double sw_sigma() { return 0.5 + std::sqrt(0.25 + kSwK * kSwK); }
+
+// Complex power as z**r evaluates it: exp(r log z).
+std::complex<double> cpow_real(std::complex<double> z, double r) {
+  return std::exp(std::complex<double>(r, 0.0) * std::log(z));
+}
+}  // namespace
+
+// getPhaseSpeed (:139-183): the three roots of the cubic
+// k^2 C^3 - En C - 2 g H0 omega / a^2 = 0 by Cardano's formula; Rossby is
+// minus the smallest magnitude, EIG the largest, WIG the smallest.
+double sw_waves_phase_speed(int wave_flag) {
+  using cd = std::complex<double>;
+  const double sigma = sw_sigma(), k = kSwK, n = kSwN;
+  const double En = kSwG * kSwH0 / (kSwA * kSwA) * ((n + sigma) * (n + sigma));
+  const double Delta0 = 3.0 * (k * k) * En;
+  const double Delta4 = -(54.0 * (k * k * k * k) * kSwG * kSwH0 * kSwOmega / (kSwA * kSwA));
+  const double r3 = 1.0 / 3.0;
+  double Cj[3];
+  for (int j = 1; j <= 3; ++j) {
+    cd D = cpow_real(cd(1.0, 0.0) * (Delta4 * Delta4 - 4.0 * (Delta0 * Delta0 * Delta0)), 0.5);
+    D = cpow_real(0.5 * (Delta4 + D), r3);
+    D = D * std::exp(2.0 * kSwPi * cd(0.0, 1.0) * (double)j * r3);
+    Cj[j - 1] = -(r3 / (k * k) * (D + Delta0 / D)).real();
+  }
+  if (wave_flag == 0) return -std::min({std::fabs(Cj[0]), std::fabs(Cj[1]), std::fabs(Cj[2])});
+  if (wave_flag == 1) return std::max({Cj[0], Cj[1], Cj[2]});
+  return std::min({Cj[0], Cj[1], Cj[2]});
+}
+
+// getPsi (:188-215) and getAmplitudes (:220-268) of the Rossby wave at the
+// full latitudes; getFields' longitude factors (:272-318) at time 0.
+void sw_waves_tables(const Mesh& m, std::vector<double>& t) {
+  const int N = m.N, M = m.M;
+  const double sigma = sw_sigma(), k = kSwK;
+  const double a3 = sigma * (sigma + 1) * (sigma + 2), a4 = a3 * (sigma + 3), a5 = a4 * (sigma + 4);
+  const double amp = 1.0e-8, r2 = 0.5, o2 = 2.0 * kSwOmega;
+  const double C = sw_waves_phase_speed(0);
+  t.assign(sw_table_words(N, M), 0.0);
+  for (int j = 0; j < M; ++j) {
+    const double lat = m.full_lat[j];
+    const double s = std::sin(lat), c = std::cos(lat), tn = std::tan(lat);
+    const double s2 = s * s, s4 = s2 * s2;
+    const double C5 = (4.0 * a5 * s4 - 20.0 * a4 * s2 + 15.0 * a3) * s / 15.0;
+    const double C5p = (4.0 * a5 * s4 - 12.0 * a4 * s2 + 3.0 * a3) * c / 3.0;
+    const double psi = amp * std::pow(c, sigma) * C5;
+    const double dpsi = amp * std::pow(c, sigma) * (-(sigma * tn * C5) + C5p);
+    const double Kp = (kSwG * kSwH0 + kSwA * kSwA * (C * C) * (c * c)) / (C * c);
+    const double Km = (kSwG * kSwH0 - kSwA * kSwA * (C * C) * (c * c)) / (C * c);
+    const double vt = std::pow(o2 * std::fabs(Km) / (c * c), r2) * psi;
+    const double ht = std::pow(o2 * std::fabs(Km) * (kSwA * kSwA) * (kSwH0 * kSwH0), r2) / Km *
+                      (dpsi + tn * (r2 * Kp / Km - o2 / C) * psi);
+    const double ut = (o2 * s / C) * vt + (kSwG / kSwA / c / C) * ht;
+    t[j] = ut;
+    t[M + j] = k * vt;
+    t[2 * M + j] = ht;
+  }
+  double* col = t.data() + 3 * (size_t)M;
+  for (int i = 0; i < N; ++i) {
+    col[i] = std::cos(k * m.half_lon[i]);
+    col[N + i] = std::cos(k * m.full_lon[i] - 0.5 * kSwPi);
+    col[2 * N + i] = std::cos(k * m.full_lon[i]);
+  }
+}
+}  // namespace gdc
+
+// src/test_cases/barotropic/shallow_water_waves_test_mod.F90:97-135
+extern "C" int gdc_ic_shallow_water_waves(int N, int M, double* u, double* v, double* gd, double* ghs,
+                                          int ld) {
+  if (!check_grid(N, M, ld) || !u || !v || !gd || !ghs) return GDC_E_CONFIG;
+  const gdc::Mesh m = gdc::make_mesh(N, M);
+  std::vector<double> t;
+  gdc::sw_waves_tables(m, t);
+  zero_field(u, ld, M); zero_field(v, ld, M - 1); zero_field(gd, ld, M); zero_field(ghs, ld, M);
+  for (int j = 0; j < M; ++j)
+    for (int i = 0; i < N; ++i) {
+      P(u, ld, i, j) = gdc::sw_u(t.data(), N, M, i, j);
+      P(gd, ld, i, j) = gdc::sw_gd(t.data(), N, M, i, j);
+      if (j < M - 1) P(v, ld, i, j) = gdc::sw_v(t.data(), N, M, i, j);
+    }
+  fill_lon_halo(u, ld, N, M); fill_lon_halo(v, ld, N, M - 1); fill_lon_halo(gd, ld, N, M);
+  return GDC_OK;
+}
+
+extern "C" double gdc_sw_waves_phase_speed(int wave_flag) { return gdc::sw_waves_phase_speed(wave_flag); }
 
 namespace gdc {
 // The random draws of gdc_ic_seeded, in its order (mountain centres, then

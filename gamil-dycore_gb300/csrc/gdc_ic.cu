@@ -1,8 +1,8 @@
 // gdc_ic.cu -- initial conditions generated in device memory (FP64), the
 // device counterparts of the gdc_ic_* host functions in gdc_host.cpp: the
-// reference's Rossby-Haurwitz wave, steady geostrophic flow and mountain
-// zonal flow test cases, and the seeded harmonic state with its optional
-// white noise.  The mesh tables and the seeded state's random draws come
+// reference's Rossby-Haurwitz wave, steady geostrophic flow, mountain zonal
+// flow and shallow-water wave test cases, and the seeded harmonic state with
+// its optional white noise.  The mesh tables and the seeded state's random draws come
 // from the host (the same values the host functions use); the per-point
 // arithmetic runs here, so a member of any size is admitted without host
 // arrays.  Compiled without FMA contraction, like the FP64 kernels.
@@ -13,7 +13,7 @@
 namespace gdc {
 namespace {
 
-constexpr double kG = 9.80616;  // src/params_mod.F90:11
+constexpr double kG = kGrav;
 constexpr int kIcThreads = 256;
 
 struct MeshView {
@@ -24,33 +24,23 @@ struct MeshView {
 
 __device__ __forceinline__ int grid_stride() { return gridDim.x * blockDim.x; }
 
-// src/test_cases/barotropic/rossby_haurwitz_wave_test_mod.F90:33-85
-__global__ void rh_kernel(MeshView m, double* u, double* v, double* gd) {
-  const double R = 4.0, omg = 7.848e-6, gd0 = 8.0e3 * kG;
-  const int N = m.N;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < m.M * N; q += grid_stride()) {
+// Separable states (Rossby-Haurwitz wave, shallow-water Rossby wave): the
+// products of the host's factor tables, with the host's own inline
+// evaluators, so the fields equal the gdc_ic_* host arrays bit for bit.
+template <int KIND>
+__global__ void separable_kernel(MeshView m, const double* t, double* u, double* v, double* gd) {
+  const int N = m.N, M = m.M;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < M * N; q += grid_stride()) {
     const int j = q / N, i = q - j * N;
-    {
-      const double cl = m.full_cos[j], sl = m.full_sin[j], lon = m.half_lon[i];
-      const double a = cl;
-      const double b = R * pow(cl, R - 1) * (sl * sl) * cos(R * lon);
-      const double c = pow(cl, R + 1) * cos(R * lon);
-      u[q] = kRadius * omg * (a + b - c);
+    if (KIND == GDC_IC_ROSSBY_HAURWITZ) {
+      u[q] = rh_u(t, N, M, i, j);
+      gd[q] = rh_gd(t, N, M, i, j);
+      if (j < m.Mh) v[q] = rh_v(t, N, M, i, j);
+    } else {
+      u[q] = sw_u(t, N, M, i, j);
+      gd[q] = sw_gd(t, N, M, i, j);
+      if (j < m.Mh) v[q] = sw_v(t, N, M, i, j);
     }
-    if (j < m.Mh) {
-      const double cl = m.half_cos[j], sl = m.half_sin[j], lon = m.full_lon[i];
-      const double a = R * pow(cl, R - 1) * sl * sin(R * lon);
-      v[q] = -kRadius * omg * a;
-    }
-    const double cl = m.full_cos[j], lon = m.full_lon[i];
-    const double a = 0.5 * omg * (2 * kOmega + omg) * (cl * cl) +
-                     0.25 * omg * omg *
-                         ((R + 1) * pow(cl, 2 * R + 2) + (2 * R * R - R - 2) * pow(cl, 2 * R) -
-                          2 * R * R * pow(cl, 2 * R - 2));
-    const double b = 2 * (kOmega + omg) * omg * pow(cl, R) * (R * R + 2 * R + 2 - (R + 1) * (R + 1) * (cl * cl)) /
-                     (R + 1) / (R + 2);
-    const double c = 0.25 * omg * omg * pow(cl, 2 * R) * ((R + 1) * (cl * cl) - R - 2);
-    gd[q] = gd0 + kRadius * kRadius * (a + b * cos(R * lon) + c * cos(2 * R * lon));
   }
 }
 
@@ -234,7 +224,10 @@ int ic_generate(const gdc_ic_spec& spec, int N, int M, const double* tables, dou
   cudaMemsetAsync(ghs, 0, (size_t)n * sizeof(double), s);
   switch (spec.kind) {
     case GDC_IC_ROSSBY_HAURWITZ:
-      rh_kernel<<<grid, kIcThreads, 0, s>>>(m, u, v, gd);
+      separable_kernel<GDC_IC_ROSSBY_HAURWITZ><<<grid, kIcThreads, 0, s>>>(m, extra, u, v, gd);
+      break;
+    case GDC_IC_SHALLOW_WATER_WAVES:
+      separable_kernel<GDC_IC_SHALLOW_WATER_WAVES><<<grid, kIcThreads, 0, s>>>(m, extra, u, v, gd);
       break;
     case GDC_IC_STEADY_GEOSTROPHIC:
       zonal_kernel<<<grid, kIcThreads, 0, s>>>(m, 2 * kPi * kRadius / (12 * 86400), 2.94e4, 0, u, v, gd, ghs);

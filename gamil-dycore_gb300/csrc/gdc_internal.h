@@ -20,6 +20,7 @@ namespace gdc {
 constexpr double kPi = 3.141592653589793238462643383279502884;
 constexpr double kOmega = 2.0 * kPi / 86400.0;
 constexpr double kRadius = 6.37122e6;
+constexpr double kGrav = 9.80616;  // src/params_mod.F90:11
 
 // ---------------------------------------------------------------- host mesh
 struct Mesh {
@@ -41,12 +42,59 @@ void seeded_draws(unsigned long long seed, int lmax, int n_mountains, std::vecto
                   std::vector<double>& clon, std::vector<double>& ag, std::vector<double>& bg,
                   std::vector<double>& ap, std::vector<double>& bp);
 
+// Separable initial conditions: per-row and per-column factor tables built
+// on the host (the transcendental functions, O(M + N) values) and the
+// per-point products, evaluated by the same inline functions on the host
+// and on the device (no FMA contraction on either), so both give the same
+// bits.  Rossby-Haurwitz wave (src/test_cases/barotropic/rossby_haurwitz_
+// wave_test_mod.F90:33-85): rows ua, ub, uc, vb, ga, gb, gc (M each; vb
+// Mh used), columns cu, sv, cg1, cg2 (N each).
+void rh_tables(const Mesh& m, std::vector<double>& t);
+GDC_HD inline size_t rh_table_words(int N, int M) { return 7 * (size_t)M + 4 * (size_t)N; }
+GDC_HD inline double rh_u(const double* t, int N, int M, int i, int j) {
+  const double omg = 7.848e-6;
+  const double* col = t + 7 * (size_t)M;
+  const double b = t[M + j] * col[i], c = t[2 * M + j] * col[i];
+  return kRadius * omg * (t[j] + b - c);
+}
+GDC_HD inline double rh_v(const double* t, int N, int M, int i, int j) {
+  const double omg = 7.848e-6;
+  const double a = t[3 * (size_t)M + j] * t[7 * (size_t)M + N + i];
+  return -kRadius * omg * a;
+}
+GDC_HD inline double rh_gd(const double* t, int N, int M, int i, int j) {
+  const double gd0 = 8.0e3 * kGrav;
+  const double* col = t + 7 * (size_t)M;
+  return gd0 + kRadius * kRadius *
+                   (t[4 * (size_t)M + j] + t[5 * (size_t)M + j] * col[2 * N + i] + t[6 * (size_t)M + j] * col[3 * N + i]);
+}
+// Shallow-water Rossby wave of Shamir and Paldor (src/test_cases/barotropic/
+// shallow_water_waves_test_mod.F90:97-135, 232-298): rows uTilde, vTilde,
+// hTilde at the full latitudes (v's half row j takes vTilde of full row j,
+// as the reference's getFields does), columns cos(k lon) at half and full
+// longitudes and cos(k lon - pi/2); gd = g h + 5e4.  Pole-row u (below
+// 1e-100 in the reference) is set to zero.
+void sw_waves_tables(const Mesh& m, std::vector<double>& t);
+double sw_waves_phase_speed(int wave_flag);
+GDC_HD inline size_t sw_table_words(int N, int M) { return 3 * (size_t)M + 3 * (size_t)N; }
+GDC_HD inline double sw_u(const double* t, int N, int M, int i, int j) {
+  return (j == 0 || j == M - 1) ? 0.0 : t[j] * t[3 * (size_t)M + i];
+}
+GDC_HD inline double sw_v(const double* t, int N, int M, int i, int j) {
+  return t[(size_t)M + j] * t[3 * (size_t)M + N + i];
+}
+GDC_HD inline double sw_gd(const double* t, int N, int M, int i, int j) {
+  return kGrav * (t[2 * (size_t)M + j] * t[3 * (size_t)M + 2 * N + i]) + 5.0e4;
+}
+
 // Device initial conditions (gdc_ic.cu): FP64 fields, interior only, lon
 // fastest: u, gd, ghs num_lat rows, v num_lat - 1.  `tables` holds the mesh
 // (full_lat, half_lat, full_lon, half_lon, full_cos, half_cos, full_sin,
-// half_sin: M, Mh, N, N, M, Mh, M, Mh values) followed, for the seeded state,
-// by the mountain centres (lat, lon) and the harmonic coefficients (gd a, b,
-// streamfunction a, b; (lmax+1)^2 each); `scratch` 2 M N + 2 doubles.
+// half_sin: M, Mh, N, N, M, Mh, M, Mh values) followed, for the separable
+// states, by their factor tables (rh_tables, sw_waves_tables) and, for the
+// seeded state, by the mountain centres (lat, lon) and the harmonic
+// coefficients (gd a, b, streamfunction a, b; (lmax+1)^2 each); `scratch`
+// 2 M N + 2 doubles.
 int ic_generate(const gdc_ic_spec& spec, int N, int M, const double* tables, double* scratch, double* u,
                 double* v, double* gd, double* ghs, void* stream);
 

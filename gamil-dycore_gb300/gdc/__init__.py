@@ -64,7 +64,7 @@ class Params(ctypes.Structure):
     ]
 
 
-IC_ROSSBY_HAURWITZ, IC_STEADY_GEOSTROPHIC, IC_MOUNTAIN_ZONAL_FLOW, IC_SEEDED = 0, 1, 2, 3
+IC_ROSSBY_HAURWITZ, IC_STEADY_GEOSTROPHIC, IC_MOUNTAIN_ZONAL_FLOW, IC_SEEDED, IC_SHALLOW_WATER_WAVES = 0, 1, 2, 3, 4
 
 
 class ICSpec(ctypes.Structure):
@@ -128,6 +128,9 @@ def lib() -> ctypes.CDLL:
                                              ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                              ctypes.c_int, ctypes.c_double, ctypes.c_double, dp, dp, dp, dp,
                                              ctypes.c_int]),
+            "gdc_ic_shallow_water_waves": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, dp, dp, dp, dp,
+                                                          ctypes.c_int]),
+            "gdc_sw_waves_phase_speed": (ctypes.c_double, [ctypes.c_int]),
             "gdc_ic_add_noise": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong, ctypes.c_double,
                                                 dp, ctypes.c_int]),
             "gdc_batch_create": (ctypes.c_int, [ctypes.POINTER(Params), ctypes.POINTER(vp)]),
@@ -280,6 +283,20 @@ def ic_seeded(N: int, M: int, seed: int = 0, lmax: int = 6, gd0: float = 8000 * 
     if rc:
         raise GdcError(rc, "gdc_ic_seeded failed")
     return u, v, gd, ghs
+
+
+def ic_shallow_water_waves(N: int, M: int):
+    """Shamir-Paldor shallow-water Rossby wave (padded layout)."""
+    u, v, gd, ghs = padded(M, N), padded(M - 1, N), padded(M, N), padded(M, N)
+    rc = lib().gdc_ic_shallow_water_waves(N, M, _ptr(u), _ptr(v), _ptr(gd), _ptr(ghs), N + 4)
+    if rc:
+        raise GdcError(rc, "gdc_ic_shallow_water_waves failed")
+    return u, v, gd, ghs
+
+
+def sw_waves_phase_speed(wave_flag: int = 0) -> float:
+    """Phase speed (rad/s) of the shallow-water wave: 0 Rossby, 1 EIG, -1 WIG."""
+    return lib().gdc_sw_waves_phase_speed(wave_flag)
 
 
 def ic_add_noise(gd: np.ndarray, N: int, M: int, seed: int, sigma: float) -> np.ndarray:

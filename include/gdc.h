@@ -206,6 +206,15 @@ int gdc_ic_seeded(int num_lon, int num_lat, unsigned long long seed, int lmax,
                   int n_mountains, double mountain_height,
                   double mountain_radius_deg, double* u, double* v,
                   double* gd, double* ghs, int ld);
+/* src/test_cases/barotropic/shallow_water_waves_test_mod.F90:97-135: the
+ * linear Rossby wave (n = 5, k = 10, gH = 5e4) of Shamir and Paldor, gd =
+ * g h + 5e4, ghs = 0.  As the reference, v's half row j takes the amplitude
+ * of full row j; pole-row u (below 1e-100 there) is zero. */
+int gdc_ic_shallow_water_waves(int num_lon, int num_lat, double* u, double* v,
+                               double* gd, double* ghs, int ld);
+/* getPhaseSpeed (same module, :139-183) in rad/s: wave_flag 0 Rossby, 1
+ * eastward and -1 westward inertia-gravity wave. */
+double gdc_sw_waves_phase_speed(int wave_flag);
 /* Adds N(0, sigma) white noise to the interior of gd (per-member seed). */
 int gdc_ic_add_noise(int num_lon, int num_lat, unsigned long long seed,
                      double sigma, double* gd, int ld);
@@ -249,7 +258,8 @@ enum {
   GDC_IC_ROSSBY_HAURWITZ = 0,
   GDC_IC_STEADY_GEOSTROPHIC = 1,
   GDC_IC_MOUNTAIN_ZONAL_FLOW = 2,
-  GDC_IC_SEEDED = 3
+  GDC_IC_SEEDED = 3,
+  GDC_IC_SHALLOW_WATER_WAVES = 4
 };
 typedef struct gdc_ic_spec {
   int kind;

@@ -1,18 +1,20 @@
 """Initial conditions generated in device memory (gdc_batch_add_ic) against
-the host generators (gdc_ic_*): the reference's three barotropic test cases
-(src/test_cases/barotropic/*_test_mod.F90) and the seeded harmonic state,
-with and without white noise.
+the host generators (gdc_ic_*): the reference's barotropic test cases
+(src/test_cases/barotropic/*_test_mod.F90: Rossby-Haurwitz wave, steady
+geostrophic flow, mountain zonal flow, shallow-water wave) and the seeded
+harmonic state, with and without white noise.
 
-Both paths evaluate the same FP64 formulas; they differ only in the last bits
-of sin/cos/pow/exp/log and in the summation order of the seeded state's RMS
-normalisation, so the fields agree to a few units in the last place: gd
-within 1e-13 of its maximum, u within 1e-12 (the seeded u is a difference
-of a streamfunction ~1e7), v within 1e-10 (v = dpsi/dlon / (a cos lat): on
-the rows next to the poles 1/cos amplifies psi's last bits).  The analytic
-zonal flows use only exact operations on the mesh and are bitwise equal.  Runs started from them stay as
-close as runs started from the host state and from the host state with gd
-perturbed by one unit in the last place: the filter's s1/s2 rescale makes
-the step itself amplify last-bit differences on some rows.
+The separable states (the reference's four) are products of host factor
+tables or exact operations on the mesh: bitwise equal, and so are runs
+started from them.  The seeded state and the noise evaluate sin, cos, exp,
+log per point and sum the RMS normalisation in another order, so they
+agree to a few units in the last place: gd within 1e-13 of its maximum, u
+within 1e-12 (the seeded u is a difference of a streamfunction ~1e7), v
+within 1e-10 (v = dpsi/dlon / (a cos lat): on the rows next to the poles
+1/cos amplifies psi's last bits).  Runs started from them stay as close as
+runs started from the host state and from the host state with gd perturbed
+by one unit in the last place: the filter's s1/s2 rescale makes the step
+itself amplify last-bit differences on some rows.
 """
 import numpy as np
 import pytest
@@ -47,6 +49,8 @@ def host_ic(kind, N, M, spec):
         ic = gdc.ic_steady_geostrophic(N, M)
     elif kind == gdc.IC_MOUNTAIN_ZONAL_FLOW:
         ic = gdc.ic_mountain_zonal_flow(N, M)
+    elif kind == gdc.IC_SHALLOW_WATER_WAVES:
+        ic = gdc.ic_shallow_water_waves(N, M)
     else:
         ic = gdc.ic_seeded(N, M, seed=spec.seed, lmax=spec.lmax, gd0=spec.gd0, gd_rms=spec.gd_rms,
                            psi_rms=spec.psi_rms, u0=spec.u0, n_mountains=spec.n_mountains,
@@ -64,7 +68,11 @@ CASES = [
     (gdc.IC_SEEDED, {"seed": 5, "n_mountains": 3, "u0": 15.0, "lmax": 9}),
     (gdc.IC_SEEDED, {"seed": 2, "noise_seed": 77, "noise_sigma": 3.0}),
     (gdc.IC_ROSSBY_HAURWITZ, {"noise_seed": 4, "noise_sigma": 10.0}),
+    (gdc.IC_SHALLOW_WATER_WAVES, {}),
 ]
+# Built from host factor tables or exact operations only: bitwise equal.
+SEPARABLE = (gdc.IC_ROSSBY_HAURWITZ, gdc.IC_STEADY_GEOSTROPHIC, gdc.IC_MOUNTAIN_ZONAL_FLOW,
+             gdc.IC_SHALLOW_WATER_WAVES)
 
 
 @pytest.mark.parametrize("N,M", [(360, 181), (200, 101)])
@@ -82,7 +90,8 @@ def test_device_ic_matches_host_fp64(native, N, M, kind, kw):
     d0 = [rel_l2(x, y) for x, y in ((du, hu), (dv, hv), (dg, hg))]
     assert rel_linf(dg, hg) < 1e-13
     assert rel_linf(du, hu) < 1e-12 and rel_linf(dv, hv) < 1e-10
-    if kind in (gdc.IC_STEADY_GEOSTROPHIC, gdc.IC_MOUNTAIN_ZONAL_FLOW):
+    exact = kind in SEPARABLE and spec.noise_sigma == 0
+    if exact:
         for x, y in ((du, hu), (dv, hv), (dg, hg)):
             assert np.array_equal(interior(x), interior(y))
     assert np.all(interior(du)[[0, -1]] == 0)  # pole-row u
@@ -100,6 +109,8 @@ def test_device_ic_matches_host_fp64(native, N, M, kind, kw):
     for x, y, z in zip(b.get_state(idv), b.get_state(ih), b.get_state(ip)):
         assert rel_l2(x, y) <= max(1e-13, 20 * rel_l2(z, y), 20 * max(d0))
         assert rel_l2(x, y) < 1e-9
+        if exact:
+            assert np.array_equal(x, y)
     b.close()
 
 
