@@ -34,7 +34,8 @@ bool uses_isp(const gdc_params& p) { return p.split_scheme == GDC_SPLIT_ISP; }
 
 // Byte layout of one member's device allocation.
 struct Layout {
-  size_t st[SL_N][3], lo[SL_N][3], td[TS_N][3], ghs, coef, rowc, twid, rowinfo, dcoef, given_u, given_v, total;
+  size_t st[SL_N][3], lo[SL_N][3], td[TS_N][3], ghs, coef, rowc, twid, rowinfo, dcoef, given_u, given_v, wadv[2],
+      total;
 };
 
 template <typename T>
@@ -67,6 +68,9 @@ Layout make_layout(const gdc_params& p, int N, int M) {
   L.dcoef = take((size_t)(3 * M) * sizeof(double));
   L.given_u = take(full * sizeof(T));
   L.given_v = take(half * sizeof(T));
+  const bool weno = p.uv_adv_scheme == GDC_ADV_WENO;
+  L.wadv[0] = weno ? take(full * sizeof(T)) : (size_t)-1;
+  L.wadv[1] = weno ? take(half * sizeof(T)) : (size_t)-1;
   L.total = off;
   return L;
 }
@@ -295,6 +299,7 @@ class Batch final : public BatchIface {
     d.dcoef = (const double*)(base + L.dcoef);
     d.given_u = (T*)(base + L.given_u);
     d.given_v = (T*)(base + L.given_v);
+    for (int k = 0; k < 2; ++k) d.wadv[k] = L.wadv[k] == (size_t)-1 ? nullptr : (T*)(base + L.wadv[k]);
     // Upload (synchronously: admission is a step-boundary operation).
     sync_stream();
     e = cudaMemset(r.dmem, 0, L.total);
@@ -829,6 +834,7 @@ class Batch final : public BatchIface {
       c = default_cols();
     }
     const bool st = strip_shape_supported(r, c);
+    if (weno() && (r != 8 || c != 32)) return fail(GDC_E_CONFIG, "set_tile: uv_adv_scheme weno runs on 8x32 tiles");
     if (!st && !tile_shape_supported(r, c))
       return fail(GDC_E_CONFIG,
                   "set_tile: supported shapes are tiles 8x32, 8x64, 4x128, 16x64 and warp strips "
@@ -851,6 +857,13 @@ class Batch final : public BatchIface {
   // CUDA events) and keeps the fastest.  Advances the members.
   int autotune(int* rr, int* cc, double* best_ms) override {
     static const int cand[][2] = {{8, 32}, {8, 64}, {16, 64}, {4, 128}, {16, 30}};
+    if (weno()) {  // one layout
+      if (int rc = set_tile(8, 32)) return rc;
+      *rr = 8;
+      *cc = 32;
+      if (best_ms) *best_ms = 0.0;
+      return GDC_OK;
+    }
     double best = 1e30;
     int br = tile_r, bc = tile_c;
     for (auto& c : cand) {
@@ -942,7 +955,26 @@ class Batch final : public BatchIface {
     int nr = 0;
     for (const auto& w : wl) nr += w.kind == 1;
     int rc = GDC_OK;
-    if (!strips)
+    if (weno() && pass != kFastPass) {
+      // the member's WENO terms first (its own flat items)
+      std::vector<FlatItem> fl;
+      const size_t n[3] = {(size_t)M * N, (size_t)M * N, (size_t)Mh * N};
+      for (int f = 1; f < 3; ++f)
+        for (size_t b = 0; b < n[f]; b += flat_chunk<T>())
+          fl.push_back(FlatItem{id, f, (int)b, (int)std::min<size_t>(flat_chunk<T>(), n[f] - b)});
+      FlatItem* dfl = nullptr;
+      if (cudaMalloc(&dfl, sizeof(FlatItem) * fl.size()) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(dwl);
+        return fail(GDC_E_OOM, "debug_tendency: cudaMalloc");
+      }
+      cudaMemcpy(dfl, fl.data(), sizeof(FlatItem) * fl.size(), cudaMemcpyHostToDevice);
+      rc = launch_weno<T>(d_mem, dfl, (int)fl.size(), a.in_slot, d_uvslot, stream);
+      cudaStreamSynchronize(stream);
+      cudaFree(dfl);
+    }
+    if (rc) {
+    } else if (!strips)
       rc = launch_stage<T>(d_mem, dwl, (int)wl.size(), P.uv_adv_scheme, tile_r, tile_c, std::max(max_n, N), a, stream);
     else {
       rc = launch_stage<T>(d_mem, dwl, nr, P.uv_adv_scheme, 8, 32, std::max(max_n, N), a, stream);
@@ -1028,8 +1060,9 @@ class Batch final : public BatchIface {
 
   // Fastest measured: FP32 16x64 tiles on the 64-member ensemble, FP64
   // 8x32 on the single 360x181 member.
-  static int default_rows() { return sizeof(T) == 4 ? 16 : 8; }
-  static int default_cols() { return sizeof(T) == 4 ? 64 : 32; }
+  int default_rows() const { return weno() ? 8 : (sizeof(T) == 4 ? 16 : 8); }
+  int default_cols() const { return weno() ? 32 : (sizeof(T) == 4 ? 64 : 32); }
+  bool weno() const { return P.uv_adv_scheme == GDC_ADV_WENO; }
 
   // The diffusion and copy kernels run on 8x32, 8x64 or 4x128 tiles.
   bool own_tile_list() const {
@@ -1305,7 +1338,9 @@ class Batch final : public BatchIface {
       cudaEventRecord(e0, stream);
     }
     int rc = GDC_OK;
-    if (!strips) {
+    if (weno() && a.pass != kFastPass) rc = launch_weno<T>(d_mem, d_flat, nflat, a.in_slot, d_uvslot, stream);
+    if (rc) {
+    } else if (!strips) {
       rc = launch_stage<T>(d_mem, d_wl, nwork, P.uv_adv_scheme, tile_r, tile_c, max_n, a, stream);
     } else if (pr) {  // timed launch by launch: one stream
       rc = launch_stage<T>(d_mem, d_wl, nrow, P.uv_adv_scheme, 8, 32, max_n, a, stream);
@@ -1596,11 +1631,8 @@ int validate_scheme(const gdc_params* p, std::string& err) {
     err = "null params";
     return GDC_E_CONFIG;
   }
-  if (p->uv_adv_scheme == GDC_ADV_WENO) {
-    err = "uv_adv_scheme 'weno' is not supported";
-    return GDC_E_CONFIG;
-  }
-  if (p->uv_adv_scheme != GDC_ADV_CENTER_DIFF && p->uv_adv_scheme != GDC_ADV_UPWIND) {
+  if (p->uv_adv_scheme != GDC_ADV_CENTER_DIFF && p->uv_adv_scheme != GDC_ADV_UPWIND &&
+      p->uv_adv_scheme != GDC_ADV_WENO) {
     err = "Unknown uv_adv_scheme";
     return GDC_E_CONFIG;
   }

@@ -193,6 +193,8 @@ struct MemberDev {
   const double* dcoef;    // FP64 diag weights: mass weight [M], full cos [M], half cos [Mh]
   T* given_u;             // u and v supplied with the state of level uvslot[member]
   T* given_v;             // (initial condition, diffusion) rather than derived
+  T* wadv[2];             // uv_adv_scheme weno: -(u_adv_lon + u_adv_lat) [M N] and
+                          // -(v_adv_lon + v_adv_lat) [Mh N] of the stage's input, else null
 };
 
 enum Field { F_GD = 0, F_IU = 1, F_IV = 2 };
@@ -334,6 +336,11 @@ int launch_stage_strips(const MemberDev<T>* mem, const WorkItem* strips, int nst
 template <typename T>
 int launch_ic_iap(const MemberDev<T>* mem, int slot, int lvl, int N, int M, const double* u, const double* v,
                   const double* gd, const double* ghs, void* stream);
+// The WENO advection terms of every member's level `in_slot` (flat items
+// of the iap u and v fields; gd items are skipped).
+template <typename T>
+int launch_weno(const MemberDev<T>* mem, const FlatItem* fl, int nflat, int in_slot, const int* uvslot,
+                void* stream);
 template <typename T>
 int launch_history(const MemberDev<T>* mem, int slot, int lvl, int given, int num_lat, double* ua, double* va,
                    double* gh, double* div, double* vor, void* stream);

@@ -354,11 +354,14 @@ struct TileView {
   __device__ __forceinline__ T ch(int k, int jj) const { return t.ch(k, jj); }
 };
 
+// `wadv`: the WENO advection term -(u_adv_lon + u_adv_lat) of this point,
+// computed beforehand by weno_kernel (uv_adv_scheme weno only).
 template <typename T, int PASS, int ADV, class S>
-__device__ __forceinline__ T point_du(const S& s, T beta_lon, T beta_lat) {
+__device__ __forceinline__ T point_du(const S& s, T beta_lon, T beta_lat, T wadv = T(0)) {
   const int j = s.j;
   T r = 0;
-  if (PASS != kFastPass) {
+  if (PASS != kFastPass && ADV == GDC_ADV_WENO) r = wadv;
+  if (PASS != kFastPass && ADV != GDC_ADV_WENO) {
     // src/dycore_mod.F90:376-392 / :393-415
     const T uc = s.u(0, 0), um = s.u(0, -1), up = s.u(0, 1);
     const T u1 = uc + um, u2 = uc + up;
@@ -399,10 +402,11 @@ __device__ __forceinline__ T point_du(const S& s, T beta_lon, T beta_lat) {
 }
 
 template <typename T, int PASS, int ADV, class S>
-__device__ __forceinline__ T point_dv(const S& s, T beta_lon, T beta_lat) {
+__device__ __forceinline__ T point_dv(const S& s, T beta_lon, T beta_lat, T wadv = T(0)) {
   const int jh = s.j;
   T r = 0;
-  if (PASS != kFastPass) {
+  if (PASS != kFastPass && ADV == GDC_ADV_WENO) r = wadv;
+  if (PASS != kFastPass && ADV != GDC_ADV_WENO) {
     // src/dycore_mod.F90:386-391 / :406-414
     const T u1 = s.u(0, -1) + s.u(1, -1);
     const T u2 = s.u(0, 0) + s.u(1, 0);
@@ -591,6 +595,176 @@ __device__ void filter_rescale(const MemberDev<T>& md, T* x, const T* __restrict
   __syncthreads();
 }
 
+// ------------------------------------------------------------- WENO
+// uv_adv_scheme weno (src/weno_mod.F90, weno_order 2): the momentum
+// advection terms of every point, written to md.wadv for the stage kernel.
+// One point per thread, straight from global memory: the reference's
+// Lax-Friedrichs split fluxes and interface fluxes are recomputed at each
+// point that reads them (the 5-point stencil and its u/v derivation are
+// cached in L1), in the reference's order of operations.  Kept as the
+// reference has them: u_adv_lon divides by half_dlon of the row's half row
+// (:153-154), u_adv_lat's correction takes v at lon i-1, i (:281-282), and
+// the split fluxes are zero on the pole and lat-halo rows (those halos are
+// never filled).
+template <typename T>
+struct WenoIn {
+  const T *gd, *iu, *iv, *gu, *gv;
+  int N, M, Mh;
+  bool given;
+  __device__ __forceinline__ int wrap(int i) const { return i < 0 ? i + N : (i >= N ? i - N : i); }
+  // u at column i (periodic), full row j; zero on the pole rows
+  __device__ __forceinline__ T u(int i, int j) const {
+    if (j < 1 || j > M - 2) return T(0);
+    i = wrap(i);
+    if (given) return gu[j * N + i];
+    const int ip = i + 1 == N ? 0 : i + 1;
+    return iu[j * N + i] * T(2) / (sqrt(gd[j * N + i]) + sqrt(gd[j * N + ip]));
+  }
+  // v at column i (periodic), half row j; zero off the half rows
+  __device__ __forceinline__ T v(int i, int j) const {
+    if (j < 0 || j > Mh - 1) return T(0);
+    i = wrap(i);
+    if (given) return gv[j * N + i];
+    return iv[j * N + i] * T(2) / (sqrt(gd[j * N + i]) + sqrt(gd[(j + 1) * N + i]));
+  }
+  __device__ __forceinline__ T iu_(int i, int j) const { return iu[j * N + wrap(i)]; }
+  __device__ __forceinline__ T iv_(int i, int j) const { return iv[j * N + wrap(i)]; }
+};
+
+// weno_2nd_order_pass (src/weno_mod.F90:249-298, coefficients :41-46)
+template <typename T>
+__device__ __forceinline__ T weno2(T fp1, T fp2, T fp3, T fn2, T fn3, T fn4) {
+  const T c11 = T(-0.5), c21 = T(1.5), c12 = T(0.5), c22 = T(0.5);
+  const T wo1 = T(1.0 / 3.0), wo2 = T(2.0 / 3.0), eps = T(1.0e-6);
+  T fs1 = c11 * fp1 + c21 * fp2, fs2 = c12 * fp2 + c22 * fp3;
+  T b1 = (fp2 - fp1) * (fp2 - fp1), b2 = (fp3 - fp2) * (fp3 - fp2);
+  T w1 = wo1 / ((eps + b1) * (eps + b1)), w2 = wo2 / ((eps + b2) * (eps + b2));
+  T sw = w1 + w2;
+  w1 = w1 / sw;
+  w2 = w2 / sw;
+  const T f = w1 * fs1 + w2 * fs2;
+  fs1 = c11 * fn4 + c21 * fn3;
+  fs2 = c12 * fn3 + c22 * fn2;
+  b1 = (fn3 - fn4) * (fn3 - fn4);
+  b2 = (fn2 - fn3) * (fn2 - fn3);
+  w1 = wo1 / ((eps + b1) * (eps + b1));
+  w2 = wo2 / ((eps + b2) * (eps + b2));
+  sw = w1 + w2;
+  w1 = w1 / sw;
+  w2 = w2 / sw;
+  return f + (w1 * fs1 + w2 * fs2);
+}
+
+// -(u_adv_lon + u_adv_lat) at u point (i, full row j), 1 <= j <= M-2
+// (src/weno_mod.F90:66-73, 102-110, 151-155; :169-177, 199-206, 225-229).
+template <typename T>
+__device__ T weno_point_u(const WenoIn<T>& s, const T* coef, int i, int j) {
+  const int M = s.M;
+  const T umax = T(20), vmax = T(20), h = T(0.5), q = T(0.25);
+  // zonal: split fluxes of row j at columns i-2..i+2
+  T fp[5], fn[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const T uk = s.u(i - 2 + k, j), ik = s.iu_(i - 2 + k, j);
+    fp[k] = h * (uk + umax) * ik;
+    fn[k] = h * (uk - umax) * ik;
+  }
+  const T fi = weno2(fp[1], fp[2], fp[3], fn[2], fn[3], fn[4]);
+  const T fim = weno2(fp[0], fp[1], fp[2], fn[1], fn[2], fn[3]);
+  const T ual = (fi - fim - (s.u(i + 1, j) - s.u(i - 1, j)) * s.iu_(i, j) * q) / coef[ch_off(CH_DLON, M) + j + 1];
+  // meridional: split fluxes of column i at rows j-2..j+2 (zero off 1..M-2)
+  T mp[5], mn[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const int r = j - 2 + k;
+    if (r >= 1 && r <= M - 2) {
+      const T vb = q * (s.v(i, r - 1) + s.v(i, r) + s.v(i + 1, r - 1) + s.v(i + 1, r));
+      const T ik = s.iu_(i, r);
+      mp[k] = h * (vb + vmax) * ik;
+      mn[k] = h * (vb - vmax) * ik;
+    } else {
+      mp[k] = T(0);
+      mn[k] = T(0);
+    }
+  }
+  const T gj = weno2(mp[1], mp[2], mp[3], mn[2], mn[3], mn[4]);
+  const T gjm = j - 1 >= 1 ? weno2(mp[0], mp[1], mp[2], mn[1], mn[2], mn[3]) : T(0);
+  const T uat = (gj - gjm - (s.v(i - 1, j) + s.v(i, j) - s.v(i - 1, j - 1) - s.v(i, j - 1)) * s.iu_(i, j) * q) /
+                coef[cf_off(CF_DLAT, M) + j];
+  return -ual - uat;
+}
+
+// -(v_adv_lon + v_adv_lat) at v point (i, half row j), 0 <= j <= Mh-1
+// (src/weno_mod.F90:75-85, 111-118, 156-158; :179-186, 208-215, 230-234).
+template <typename T>
+__device__ T weno_point_v(const WenoIn<T>& s, const T* coef, int i, int j) {
+  const int M = s.M, Mh = s.Mh;
+  const T umax = T(20), vmax = T(20), h = T(0.5), q = T(0.25);
+  T fp[5], fn[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const int c = i - 2 + k;
+    const T ub = q * (s.u(c - 1, j) + s.u(c - 1, j + 1) + s.u(c, j) + s.u(c, j + 1));
+    const T ik = s.iv_(c, j);
+    fp[k] = h * (ub + umax) * ik;
+    fn[k] = h * (ub - umax) * ik;
+  }
+  const T fi = weno2(fp[1], fp[2], fp[3], fn[2], fn[3], fn[4]);
+  const T fim = weno2(fp[0], fp[1], fp[2], fn[1], fn[2], fn[3]);
+  const T val = (fi - fim - (s.u(i, j) + s.u(i, j + 1) - s.u(i - 1, j) - s.u(i - 1, j + 1)) * s.iv_(i, j) * q) /
+                coef[ch_off(CH_DLON, M) + j + 1];
+  T mp[5], mn[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const int r = j - 2 + k;
+    if (r >= 0 && r <= Mh - 1) {
+      const T vk = s.v(i, r), ik = s.iv_(i, r);
+      mp[k] = h * (vk + vmax) * ik;
+      mn[k] = h * (vk - vmax) * ik;
+    } else {
+      mp[k] = T(0);
+      mn[k] = T(0);
+    }
+  }
+  const T gj = weno2(mp[1], mp[2], mp[3], mn[2], mn[3], mn[4]);
+  const T gjm = j - 1 >= 0 ? weno2(mp[0], mp[1], mp[2], mn[1], mn[2], mn[3]) : T(0);
+  const T vat = (gj - gjm - (s.v(i, j + 1) - s.v(i, j - 1)) * s.iv_(i, j) * q) / coef[ch_off(CH_DLAT, M) + j + 1];
+  return -val - vat;
+}
+
+// One flat item of a member's iap u or iap v field per block (gd items
+// return at once): the WENO terms of the stage's input level.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    weno_kernel(const MemberDev<T>* __restrict__ mems, const FlatItem* __restrict__ fl, int in_slot,
+                const int* __restrict__ uvslot) {
+  const FlatItem w = fl[blockIdx.x];
+  if (w.field == F_GD) return;
+  const MemberDev<T>& md = mems[w.member];
+  WenoIn<T> s;
+  s.gd = md.st[in_slot][F_GD];
+  s.iu = md.st[in_slot][F_IU];
+  s.iv = md.st[in_slot][F_IV];
+  s.gu = md.given_u;
+  s.gv = md.given_v;
+  s.N = md.N;
+  s.M = md.M;
+  s.Mh = md.Mh;
+  s.given = uvslot && uvslot[w.member] == in_slot;
+  const int N = md.N;
+  T* out = md.wadv[w.field == F_IU ? 0 : 1];
+  for (int k = threadIdx.x; k < w.count; k += kThreads) {
+    const int q = w.begin + k, j = q / N, i = q - j * N;
+    T r = T(0);
+    if (w.field == F_IU) {
+      if (j >= 1 && j <= md.M - 2) r = weno_point_u(s, md.coef, i, j);
+    } else {
+      r = weno_point_v(s, md.coef, i, j);
+    }
+    out[q] = r;
+  }
+}
+
 // --------------------------------------------------------- stage kernel
 
 // One bulk tile (rows j0..j0+rows-1, all ordinary; columns i0..i0+cols-1).
@@ -635,8 +809,13 @@ __device__ __forceinline__ void bulk_tile(const MemberDev<T>& md, const StageArg
     const int j = w.j0 + r, o = ob + k * N;
     const int p = TL::pos(r + 1, c + 1);
     const TileView<T, TL> sv{t, p, j};
-    const T du = point_du<T, PASS, ADV>(sv, ub_lon, ub_lat);
-    const T dv = point_dv<T, PASS, ADV>(sv, ub_lon, ub_lat);
+    T wu = T(0), wv = T(0);
+    if (ADV == GDC_ADV_WENO && PASS != kFastPass) {
+      wu = md.wadv[0][o];
+      wv = md.wadv[1][o];
+    }
+    const T du = point_du<T, PASS, ADV>(sv, ub_lon, ub_lat, wu);
+    const T dv = point_dv<T, PASS, ADV>(sv, ub_lon, ub_lat, wv);
     const T dg = point_dgd<T, PASS>(sv);
     if (UF == UF_PREDICT_IN) {
       // update_state from the input level (src/dycore_mod.F90:609-633)
@@ -1088,8 +1267,10 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
         const int p = TR::pos(1, c + 1);
         const int i = c0 + c;
         const TileView<T, TR> sv{t, p, j};
-        if (want_u) xr[F_IU][i] = has_du ? point_du<T, PASS, ADV>(sv, ub_lon, ub_lat) : T(0);
-        if (want_v) xr[F_IV][i] = point_dv<T, PASS, ADV>(sv, ub_lon, ub_lat);
+        const bool wl = ADV == GDC_ADV_WENO && PASS != kFastPass;
+        if (want_u)
+          xr[F_IU][i] = has_du ? point_du<T, PASS, ADV>(sv, ub_lon, ub_lat, wl ? md.wadv[0][j * N + i] : T(0)) : T(0);
+        if (want_v) xr[F_IV][i] = point_dv<T, PASS, ADV>(sv, ub_lon, ub_lat, wl ? md.wadv[1][j * N + i] : T(0));
         if (!want_g) continue;
         if (south || north) {
           // src/dycore_mod.F90:572-596: sp += (ig(j)+ig(j+1)) iv(j);
@@ -1760,6 +1941,16 @@ static int launch_stage_shape(const MemberDev<T>* mem, const WorkItem* wl, int n
   return GDC_E_CONFIG;
 }
 
+// WENO members use 8x32 tiles only (one instantiation per pass; the fast
+// pass has no advection and runs the centred kernel).
+template <typename T>
+static int launch_stage_weno(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int max_n, const StageArgs& a,
+                             cudaStream_t s) {
+  if (a.pass == kAllPass) return launch_stage_t<T, kAllPass, GDC_ADV_WENO, 8, 32>(mem, wl, nwork, max_n, a, s);
+  if (a.pass == kSlowPass) return launch_stage_t<T, kSlowPass, GDC_ADV_WENO, 8, 32>(mem, wl, nwork, max_n, a, s);
+  return launch_stage_t<T, kFastPass, GDC_ADV_CENTER_DIFF, 8, 32>(mem, wl, nwork, max_n, a, s);
+}
+
 template <typename T>
 int launch_stage(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int adv, int tile_rows, int tile_cols,
                  int max_n, const StageArgs& args, void* stream) {
@@ -1767,6 +1958,8 @@ int launch_stage(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int adv
   cudaStream_t s = (cudaStream_t)stream;
   StageArgs a = args;
   a.form = update_form(args);
+  if (adv == GDC_ADV_WENO)
+    return tile_rows == 8 && tile_cols == 32 ? launch_stage_weno<T>(mem, wl, nwork, max_n, a, s) : GDC_E_CONFIG;
   if (tile_rows == 8 && tile_cols == 32) return launch_stage_shape<T, 8, 32>(mem, wl, nwork, adv, max_n, a, s);
   if (tile_rows == 8 && tile_cols == 64) return launch_stage_shape<T, 8, 64>(mem, wl, nwork, adv, max_n, a, s);
   if (tile_rows == 16 && tile_cols == 64) return launch_stage_shape<T, 16, 64>(mem, wl, nwork, adv, max_n, a, s);
@@ -1845,6 +2038,14 @@ int launch_ic_iap(const MemberDev<T>* mem, int slot, int lvl, int N, int M, cons
                   const double* gd, const double* ghs, void* stream) {
   const int n = N * M, grid = (n + kThreads - 1) / kThreads;
   ic_iap_kernel<T><<<grid, kThreads, 0, (cudaStream_t)stream>>>(mem, slot, lvl, u, v, gd, ghs);
+  return check_launch();
+}
+
+template <typename T>
+int launch_weno(const MemberDev<T>* mem, const FlatItem* fl, int nflat, int in_slot, const int* uvslot,
+                void* stream) {
+  if (nflat <= 0) return GDC_OK;
+  weno_kernel<T><<<nflat, kThreads, 0, (cudaStream_t)stream>>>(mem, fl, in_slot, uvslot);
   return check_launch();
 }
 

@@ -40,7 +40,7 @@ extern "C" {
 #define GDC_SPLIT_ISP 3
 #define GDC_ADV_CENTER_DIFF 0
 #define GDC_ADV_UPWIND 1
-#define GDC_ADV_WENO 2 /* rejected with GDC_E_CONFIG */
+#define GDC_ADV_WENO 2 /* weno_order 2, src/weno_mod.F90 (8x32 tiles) */
 #define GDC_FP64 0     /* plain path: everything in FP64                   */
 #define GDC_FP32 1     /* FP32 state/tendencies, compensated time levels,
                           FP64 pole-cap sums and mass/energy integrals      */

@@ -34,7 +34,7 @@
 
 enum { NO_SPLIT = 0, CSP2 = 2, ISP = 3 };
 enum { ALL_PASS = 0, FAST_PASS = 1, SLOW_PASS = 2 };
-enum { CENTER_DIFF = 0, UPWIND = 1 };
+enum { CENTER_DIFF = 0, UPWIND = 1, WENO = 2 };
 
 /* src/types_mod.F90:58-72 */
 enum {
@@ -77,6 +77,11 @@ struct gdo_model {
   int *flag_full, *flag_half;    /* 1-based */
   double *ffac_full, *ffac_half; /* [lat][N], 1-based lat, 0-based lon */
   double *ctab, *stab;           /* cos/sin(2 pi m / N), m = 0..N-1 */
+  /* WENO scratch, src/weno_mod.F90:26-31: split and interface fluxes
+   * (u-shaped fp_u, fn_u, f_u; v-shaped fp_v, fn_v, f_v).  Zeroed once
+   * (parallel_allocate, src/parallel_mod.F90:312-313); the pole and
+   * lat-halo rows are never written afterwards. */
+  double *w_fpu, *w_fnu, *w_fu, *w_fpv, *w_fnv, *w_fv;
   /* diffusion scratch, src/diffusion_mod.F90:20-26 */
   double *d_ud, *d_vd, *d_gdd, *d_u, *d_v, *d_gd;
   /* time_mod indices and diag */
@@ -313,6 +318,10 @@ gdo_model* gdo_create(int num_lon, int num_lat, double time_step_size,
   m->d_ud = zalloc(full_sz(m)); m->d_gdd = zalloc(full_sz(m));
   m->d_u = zalloc(full_sz(m)); m->d_gd = zalloc(full_sz(m));
   m->d_vd = zalloc(half_sz(m)); m->d_v = zalloc(half_sz(m));
+  if (m->adv == WENO) {
+    m->w_fpu = zalloc(full_sz(m)); m->w_fnu = zalloc(full_sz(m)); m->w_fu = zalloc(full_sz(m));
+    m->w_fpv = zalloc(half_sz(m)); m->w_fnv = zalloc(half_sz(m)); m->w_fv = zalloc(half_sz(m));
+  }
   m->old = 1; m->new_ = 2; /* src/time_mod.F90:68-69 */
   m->last_beta = 1.0;
   return m;
@@ -333,7 +342,8 @@ void gdo_destroy(gdo_model* m) {
                     m->full_sin, m->half_sin, m->full_f, m->half_f, m->full_c,
                     m->half_c, m->full_dlon, m->half_dlon, m->full_dlat,
                     m->half_dlat, m->ghs, m->ffac_full, m->ffac_half, m->ctab,
-                    m->stab, m->d_ud, m->d_vd, m->d_gdd, m->d_u, m->d_v, m->d_gd};
+                    m->stab, m->d_ud, m->d_vd, m->d_gdd, m->d_u, m->d_v, m->d_gd,
+                    m->w_fpu, m->w_fnu, m->w_fu, m->w_fpv, m->w_fnv, m->w_fv};
   for (size_t k = 0; k < sizeof(bufs) / sizeof(bufs[0]); ++k) free(bufs[k]);
   for (int k = 0; k < 4; ++k) {
     state_t* s = &m->state_mem[k];
@@ -430,9 +440,135 @@ void gdo_filter_flags(const gdo_model* m, int* out_full, int* out_half,
 
 /* ---------------------------------------------------------- operators */
 
+/* ------------------------------------------------------------ WENO
+ * src/weno_mod.F90 with weno_order = 2, restated as the reference runs it:
+ * Lax-Friedrichs split fluxes with u_max = v_max = 20, the two-stencil
+ * weno_2nd_order_pass, and the reference's index choices kept as they are:
+ * u_adv_lon divides by coef%half_dlon(j) (:153-154), u_adv_lat's correction
+ * term takes v at lon i-1, i (:281-282), and the lat halos of the split
+ * fluxes are never filled (parallel_fill_halo fills lon halos only,
+ * src/parallel_mod.F90:466-524), so the pole and lat-halo rows of every
+ * split and interface flux are zero. */
+#define WENO_EPS 1.0e-6
+#define WENO_UMAX 20.0
+#define WENO_VMAX 20.0
+
+/* src/weno_mod.F90:249-298 (coefficients :41-46) */
+static double weno_2nd_order_pass(double fp1, double fp2, double fp3, double fn2, double fn3, double fn4) {
+  const double c11 = -(1.0 / 2.0), c21 = 3.0 / 2.0, c12 = 1.0 / 2.0, c22 = 1.0 / 2.0;
+  const double wo1 = 1.0 / 3.0, wo2 = 2.0 / 3.0;
+  double fs1 = c11 * fp1 + c21 * fp2, fs2 = c12 * fp2 + c22 * fp3;
+  double b1 = (fp2 - fp1) * (fp2 - fp1), b2 = (fp3 - fp2) * (fp3 - fp2);
+  double w1 = wo1 / ((WENO_EPS + b1) * (WENO_EPS + b1)), w2 = wo2 / ((WENO_EPS + b2) * (WENO_EPS + b2));
+  double sw = w1 + w2;
+  w1 = w1 / sw;
+  w2 = w2 / sw;
+  double f = w1 * fs1 + w2 * fs2;
+  fs1 = c11 * fn4 + c21 * fn3;
+  fs2 = c12 * fn3 + c22 * fn2;
+  b1 = (fn3 - fn4) * (fn3 - fn4);
+  b2 = (fn2 - fn3) * (fn2 - fn3);
+  w1 = wo1 / ((WENO_EPS + b1) * (WENO_EPS + b1));
+  w2 = wo2 / ((WENO_EPS + b2) * (WENO_EPS + b2));
+  sw = w1 + w2;
+  w1 = w1 / sw;
+  w2 = w2 / sw;
+  return f + (w1 * fs1 + w2 * fs2);
+}
+
+/* src/weno_mod.F90:58-159 */
+static void weno_zonal(gdo_model* m, const state_t* s, tend_t* t) {
+  int N = m->N, M = m->M, Mh = m->Mh;
+  double *fpu = m->w_fpu, *fnu = m->w_fnu, *fu = m->w_fu, *fpv = m->w_fpv, *fnv = m->w_fnv, *fv = m->w_fv;
+  double *ual = t->a[T_U_ADV_LON], *val = t->a[T_V_ADV_LON];
+  for (int j = 2; j <= M - 1; ++j)
+    for (int i = 1; i <= N; ++i) {
+      AT(m, fpu, i, j) = 0.5 * (AT(m, s->u, i, j) + WENO_UMAX) * AT(m, s->iu, i, j);
+      AT(m, fnu, i, j) = 0.5 * (AT(m, s->u, i, j) - WENO_UMAX) * AT(m, s->iu, i, j);
+    }
+  fill_halo(m, fpu, 0);
+  fill_halo(m, fnu, 0);
+  for (int j = 1; j <= Mh; ++j)
+    for (int i = 1; i <= N; ++i) {
+      double u = 0.25 * (AT(m, s->u, i - 1, j) + AT(m, s->u, i - 1, j + 1) + AT(m, s->u, i, j) + AT(m, s->u, i, j + 1));
+      AT(m, fpv, i, j) = 0.5 * (u + WENO_UMAX) * AT(m, s->iv, i, j);
+      AT(m, fnv, i, j) = 0.5 * (u - WENO_UMAX) * AT(m, s->iv, i, j);
+    }
+  fill_halo(m, fpv, 1);
+  fill_halo(m, fnv, 1);
+  for (int j = 2; j <= M - 1; ++j)
+    for (int i = 1; i <= N; ++i)
+      AT(m, fu, i, j) = weno_2nd_order_pass(AT(m, fpu, i - 1, j), AT(m, fpu, i, j), AT(m, fpu, i + 1, j),
+                                            AT(m, fnu, i, j), AT(m, fnu, i + 1, j), AT(m, fnu, i + 2, j));
+  for (int j = 1; j <= Mh; ++j)
+    for (int i = 1; i <= N; ++i)
+      AT(m, fv, i, j) = weno_2nd_order_pass(AT(m, fpv, i - 1, j), AT(m, fpv, i, j), AT(m, fpv, i + 1, j),
+                                            AT(m, fnv, i, j), AT(m, fnv, i + 1, j), AT(m, fnv, i + 2, j));
+  fill_halo(m, fu, 0);
+  fill_halo(m, fv, 1);
+  for (int j = 2; j <= M - 1; ++j)
+    for (int i = 1; i <= N; ++i)
+      AT(m, ual, i, j) = (AT(m, fu, i, j) - AT(m, fu, i - 1, j) -
+                          (AT(m, s->u, i + 1, j) - AT(m, s->u, i - 1, j)) * AT(m, s->iu, i, j) * 0.25) /
+                         m->half_dlon[j];
+  for (int j = 1; j <= Mh; ++j)
+    for (int i = 1; i <= N; ++i)
+      AT(m, val, i, j) = (AT(m, fv, i, j) - AT(m, fv, i - 1, j) -
+                          (AT(m, s->u, i, j) + AT(m, s->u, i, j + 1) - AT(m, s->u, i - 1, j) -
+                           AT(m, s->u, i - 1, j + 1)) * AT(m, s->iv, i, j) * 0.25) /
+                         m->half_dlon[j];
+}
+
+/* src/weno_mod.F90:161-247 */
+static void weno_meridional(gdo_model* m, const state_t* s, tend_t* t) {
+  int N = m->N, M = m->M, Mh = m->Mh;
+  double *fpu = m->w_fpu, *fnu = m->w_fnu, *fu = m->w_fu, *fpv = m->w_fpv, *fnv = m->w_fnv, *fv = m->w_fv;
+  double *ual = t->a[T_U_ADV_LAT], *val = t->a[T_V_ADV_LAT];
+  for (int j = 2; j <= M - 1; ++j)
+    for (int i = 1; i <= N; ++i) {
+      double v = 0.25 * (AT(m, s->v, i, j - 1) + AT(m, s->v, i, j) + AT(m, s->v, i + 1, j - 1) + AT(m, s->v, i + 1, j));
+      AT(m, fpu, i, j) = 0.5 * (v + WENO_VMAX) * AT(m, s->iu, i, j);
+      AT(m, fnu, i, j) = 0.5 * (v - WENO_VMAX) * AT(m, s->iu, i, j);
+    }
+  fill_halo(m, fpu, 0);
+  fill_halo(m, fnu, 0);
+  for (int j = 1; j <= Mh; ++j)
+    for (int i = 1; i <= N; ++i) {
+      AT(m, fpv, i, j) = 0.5 * (AT(m, s->v, i, j) + WENO_VMAX) * AT(m, s->iv, i, j);
+      AT(m, fnv, i, j) = 0.5 * (AT(m, s->v, i, j) - WENO_VMAX) * AT(m, s->iv, i, j);
+    }
+  fill_halo(m, fpv, 1);
+  fill_halo(m, fnv, 1);
+  for (int j = 2; j <= M - 1; ++j)
+    for (int i = 1; i <= N; ++i)
+      AT(m, fu, i, j) = weno_2nd_order_pass(AT(m, fpu, i, j - 1), AT(m, fpu, i, j), AT(m, fpu, i, j + 1),
+                                            AT(m, fnu, i, j), AT(m, fnu, i, j + 1), AT(m, fnu, i, j + 2));
+  for (int j = 1; j <= Mh; ++j)
+    for (int i = 1; i <= N; ++i)
+      AT(m, fv, i, j) = weno_2nd_order_pass(AT(m, fpv, i, j - 1), AT(m, fpv, i, j), AT(m, fpv, i, j + 1),
+                                            AT(m, fnv, i, j), AT(m, fnv, i, j + 1), AT(m, fnv, i, j + 2));
+  fill_halo(m, fu, 0);
+  fill_halo(m, fv, 1);
+  for (int j = 2; j <= M - 1; ++j)
+    for (int i = 1; i <= N; ++i)
+      AT(m, ual, i, j) = (AT(m, fu, i, j) - AT(m, fu, i, j - 1) -
+                          (AT(m, s->v, i - 1, j) + AT(m, s->v, i, j) - AT(m, s->v, i - 1, j - 1) -
+                           AT(m, s->v, i, j - 1)) * AT(m, s->iu, i, j) * 0.25) /
+                         m->full_dlat[j];
+  for (int j = 1; j <= Mh; ++j)
+    for (int i = 1; i <= N; ++i)
+      AT(m, val, i, j) = (AT(m, fv, i, j) - AT(m, fv, i, j - 1) -
+                          (AT(m, s->v, i, j + 1) - AT(m, s->v, i, j - 1)) * AT(m, s->iv, i, j) * 0.25) /
+                         m->half_dlat[j];
+}
+
 /* src/dycore_mod.F90:367-420 */
 static void zonal_momentum_advection(gdo_model* m, const state_t* s, tend_t* t) {
   int N = m->N, M = m->M, Mh = m->Mh;
+  if (m->adv == WENO) {
+    weno_zonal(m, s, t);
+    return;
+  }
   double *ual = t->a[T_U_ADV_LON], *val = t->a[T_V_ADV_LON];
   for (int j = 2; j <= M - 1; ++j)
     for (int i = 1; i <= N; ++i) {
@@ -473,6 +609,10 @@ static void zonal_momentum_advection(gdo_model* m, const state_t* s, tend_t* t) 
  * a zero lat-halo v, so the pads hold 0.0 and the product is 0. */
 static void meridional_momentum_advection(gdo_model* m, const state_t* s, tend_t* t) {
   int N = m->N, M = m->M, Mh = m->Mh;
+  if (m->adv == WENO) {
+    weno_meridional(m, s, t);
+    return;
+  }
   double *ual = t->a[T_U_ADV_LAT], *val = t->a[T_V_ADV_LAT];
   const double* hc = m->half_cos;
   for (int j = 2; j <= M - 1; ++j)

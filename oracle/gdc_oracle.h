@@ -28,7 +28,7 @@ typedef struct gdo_model gdo_model;
 
 /* split_scheme: 0 = none (also csp1, which the reference routes to the
  * no-split path), 2 = csp2, 3 = isp.  uv_adv_scheme: 0 = center_diff,
- * 1 = upwind.  cutoff: 20 entries of zonal_tend_filter_cutoff_wavenumber. */
+ * 1 = upwind, 2 = weno (weno_order 2).  cutoff: 20 entries of zonal_tend_filter_cutoff_wavenumber. */
 gdo_model* gdo_create(int num_lon, int num_lat, double time_step_size,
                       int subcycles, int split_scheme, int qcon_modified,
                       int uv_adv_scheme, double upwind_lon_beta,

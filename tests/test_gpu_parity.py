@@ -26,7 +26,7 @@ def pair(p, ic):
     return m, o
 
 
-@pytest.mark.parametrize("adv", [0, 1])
+@pytest.mark.parametrize("adv", [gdc.ADV_CENTER_DIFF, gdc.ADV_UPWIND, gdc.ADV_WENO])
 @pytest.mark.parametrize("pass_", [0, 1, 2])
 def test_tendency_parity(native, pass_, adv):
     N, M = 360, 181
@@ -42,7 +42,7 @@ def test_tendency_parity(native, pass_, adv):
 
 
 @pytest.mark.parametrize("split,adv", [(gdc.SPLIT_NONE, 0), (gdc.SPLIT_CSP2, 0), (gdc.SPLIT_ISP, 0),
-                                       (gdc.SPLIT_CSP2, 1)])
+                                       (gdc.SPLIT_CSP2, 1), (gdc.SPLIT_NONE, gdc.ADV_WENO)])
 def test_step_parity(native, split, adv):
     N, M = 180, 91
     # Without splitting the gravity-wave step must satisfy the CFL limit of
@@ -176,3 +176,48 @@ def test_device_ic_run_parity_shallow_water_wave(native):
         assert np.array_equal(interior(a), interior(r))
     assert b.diag(mid) == o.diag()
     b.close()
+
+
+def test_weno_csp2_blows_up_at_the_oracles_step(native):
+    """The reference's WENO (zero split fluxes on the pole rows, no lat
+    halos) is unstable under csp2 splitting: the oracle's total energy turns
+    NaN at step 5 on this state, and the CUDA path stops at the same step."""
+    N, M = 180, 91
+    p = scheme(gdc, N, M, 480.0, split=gdc.SPLIT_CSP2, cutoff=(3, 3, 3), adv=gdc.ADV_WENO)
+    ic = gdc.ic_seeded(N, M, seed=2)
+    m, o = pair(p, ic)
+    bad = next(k for k in range(1, 13) if o.step(1) != 0)
+    with pytest.raises(gdc.GdcError, match=f"NaN at step {bad}"):
+        m.run(12)
+    m.close()
+
+
+def test_weno_batch_mixed_grids_parity_and_fp32(native):
+    """uv_adv_scheme weno in a batch of two grids (no splitting, dt 90 s:
+    stable for these 12 steps): each FP64 member is bitwise the oracle's run
+    (diffusion on, so the given-u/v path is exercised after each diffusion
+    step); FP32 members stay within 1e-5 (gd relative L2) of FP64; other tile
+    shapes are refused."""
+    runs = {}
+    grids = [(180, 91, 90.0), (200, 101, 90.0)]
+    for prec in (gdc.FP64, gdc.FP32):
+        p = scheme(gdc, 180, 91, 90.0, split=gdc.SPLIT_NONE, adv=gdc.ADV_WENO, cutoff=(3, 3, 3, 3), diffusion=True,
+                   precision=prec)
+        b = gdc.Batch(p)
+        with pytest.raises(gdc.GdcError):
+            b.set_tile(16, 64)
+        ids = [b.add(N, M, dt, 12, *gdc.ic_seeded(N, M, seed=N)) for N, M, dt in grids]
+        b.step(12)
+        b.sync()
+        runs[prec] = [b.get_state(i) for i in ids]
+        b.close()
+    for (N, M, dt), st in zip(grids, runs[gdc.FP64]):
+        o = OracleModel.from_params(scheme(gdc, N, M, dt, split=gdc.SPLIT_NONE, adv=gdc.ADV_WENO, cutoff=(3, 3, 3, 3),
+                                           diffusion=True))
+        o.set_state(*gdc.ic_seeded(N, M, seed=N))
+        o.step(12)
+        s = o.get_state()
+        for a, r in zip(st, (s["u"], s["v"], s["gd"])):
+            assert np.array_equal(interior(a), interior(r))
+    for a, b in zip(runs[gdc.FP32], runs[gdc.FP64]):
+        assert rel_l2(a[2], b[2]) <= 1e-5

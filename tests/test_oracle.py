@@ -174,3 +174,109 @@ def test_history_fields_known_answers():
     assert h["u_a"][5, 2] == 0.5 * (u[5, 2] + u[5, N + 1])
     assert np.array_equal(h["v_a"][2, 2:N + 2], 0.5 * v[2, 2:N + 2])          # south pole row
     assert np.array_equal(h["v_a"][M + 1, 2:N + 2], 0.5 * v[M, 2:N + 2])      # north pole row
+
+
+def _weno2(fp1, fp2, fp3, fn2, fn3, fn4):
+    """weno_2nd_order_pass (src/weno_mod.F90:249-298) restated with numpy."""
+    eps = 1.0e-6
+
+    def part(fs1, fs2, b1, b2):  # stencil fluxes, smoothness indicators
+        w1 = (1.0 / 3.0) / (eps + b1) ** 2
+        w2 = (2.0 / 3.0) / (eps + b2) ** 2
+        sw = w1 + w2
+        return (w1 / sw) * fs1 + (w2 / sw) * fs2
+
+    f = part(-0.5 * fp1 + 1.5 * fp2, 0.5 * fp2 + 0.5 * fp3, (fp2 - fp1) ** 2, (fp3 - fp2) ** 2)
+    return f + part(-0.5 * fn4 + 1.5 * fn3, 0.5 * fn3 + 0.5 * fn2, (fn3 - fn4) ** 2, (fn2 - fn3) ** 2)
+
+
+def weno_terms(s, N, M):
+    """-(u_adv_lon + u_adv_lat), -(v_adv_lon + v_adv_lat) of src/weno_mod.F90
+    (weno_order 2) restated with numpy on 0-based interior arrays: zero
+    split fluxes off the interior rows, u_adv_lon over half_dlon."""
+    Mh, A = M - 1, 6.37122e6
+    dlon, dlat = 2 * np.pi / N, np.pi / Mh
+    full_lat = -0.5 * np.pi + np.arange(M) * dlat
+    full_lat[-1] = 0.5 * np.pi
+    half_lat = full_lat[:-1] + 0.5 * dlat
+    hdlon = (A * dlon * np.cos(half_lat))[:, None]
+    fdlat = (A * dlat * np.cos(full_lat))[:, None]
+    hdlat = (A * dlat * np.cos(half_lat))[:, None]
+    u, v, iu, iv = (interior(s[k]) for k in ("u", "v", "iu", "iv"))
+    sh = lambda a, k: np.roll(a, -k, axis=1)  # a[:, i + k]
+    w = lambda f, g, k: _weno2(sh(f, k - 1), sh(f, k), sh(f, k + 1), sh(g, k), sh(g, k + 1), sh(g, k + 2))
+    # zonal, u points
+    fp, fn = 0.5 * (u + 20.0) * iu, 0.5 * (u - 20.0) * iu
+    fu = w(fp, fn, 0)
+    ual = (fu - sh(fu, -1) - (sh(u, 1) - sh(u, -1)) * iu * 0.25)[:Mh] / hdlon
+    # zonal, v points
+    um = sh(u, -1)
+    ub = 0.25 * (um[:-1] + um[1:] + u[:-1] + u[1:])
+    fpv, fnv = 0.5 * (ub + 20.0) * iv, 0.5 * (ub - 20.0) * iv
+    fv = w(fpv, fnv, 0)
+    val = (fv - sh(fv, -1) - (u[:-1] + u[1:] - um[:-1] - um[1:]) * iv * 0.25) / hdlon
+    # meridional, u points: split fluxes on rows 1..M-2, zero elsewhere
+    pad = lambda a: np.vstack([np.zeros((2, N)), a, np.zeros((2, N))])  # row r -> r + 2
+    vb = np.zeros((M, N))
+    vs = sh(v, 1)
+    vb[1:M - 1] = 0.25 * (v[:-1] + v[1:] + vs[:-1] + vs[1:])
+    mp, mn = 0.5 * (vb + 20.0) * iu, 0.5 * (vb - 20.0) * iu
+    mp[[0, M - 1]] = 0.0
+    mn[[0, M - 1]] = 0.0
+    P, Q = pad(mp), pad(mn)
+    g = np.zeros((M + 4, N))
+    for r in range(1, M - 1):
+        g[r + 2] = _weno2(P[r + 1], P[r + 2], P[r + 3], Q[r + 2], Q[r + 3], Q[r + 4])
+    vm = sh(v, -1)
+    uat = np.zeros((M, N))
+    for j in range(1, M - 1):
+        uat[j] = (g[j + 2] - g[j + 1] - (vm[j] + v[j] - vm[j - 1] - v[j - 1]) * iu[j] * 0.25) / fdlat[j]
+    # meridional, v points
+    pv, nv = pad(0.5 * (v + 20.0) * iv), pad(0.5 * (v - 20.0) * iv)
+    gv = np.zeros((Mh + 4, N))
+    for r in range(Mh):
+        gv[r + 2] = _weno2(pv[r + 1], pv[r + 2], pv[r + 3], nv[r + 2], nv[r + 3], nv[r + 4])
+    V = pad(v)
+    vat = np.zeros((Mh, N))
+    for j in range(Mh):
+        vat[j] = (gv[j + 2] - gv[j + 1] - (V[j + 3] - V[j + 1]) * iv[j] * 0.25) / hdlat[j]
+    du = np.zeros((M, N))
+    du[1:M - 1] = -ual[1:M - 1] - uat[1:M - 1]
+    return du, -val - vat
+
+
+@pytest.mark.parametrize("seed", [6, 9])
+def test_weno_tendency_matches_restatement(seed):
+    """The oracle's WENO advection (slow pass, filter off) against a numpy
+    restatement of src/weno_mod.F90 with the reference's index choices."""
+    N, M = 72, 37
+    u, v, gd, ghs = _seeded(N, M, seed=seed)
+    o = OracleModel(N, M, 600.0, subcycles=4, split_scheme=2, uv_adv_scheme=2, use_zonal_tend_filter=0,
+                    cutoff=[])
+    o.set_state(u, v, gd, ghs)
+    du, dv, dgd = o.tendency(2)
+    ru, rv = weno_terms(o.get_state(), N, M)
+    assert np.max(np.abs(interior(du) - ru)) <= 1e-12 * np.max(np.abs(ru))
+    assert np.max(np.abs(interior(dv) - rv)) <= 1e-12 * np.max(np.abs(rv))
+    assert np.all(interior(dgd) == 0)
+
+
+def test_weno_uniform_zonal_flow_known_answers():
+    """u = u0 cos(lat), v = 0 (steady geostrophic state): iap v is zero, so
+    every v-point split flux and term vanishes exactly; every u-point input
+    is constant along a row, so the zonal terms vanish (f_u(i) = f_u(i-1)
+    exactly) and du is the same in every column of a row; the meridional
+    term is nonzero (iap u varies with latitude)."""
+    import gdc
+    N, M = 72, 37
+    u, v, gd, ghs = gdc.ic_steady_geostrophic(N, M)
+    o = OracleModel(N, M, 600.0, subcycles=4, split_scheme=2, uv_adv_scheme=2, use_zonal_tend_filter=0,
+                    cutoff=[])
+    o.set_state(u, v, gd, ghs)
+    du, dv, _ = o.tendency(2)
+    assert np.all(interior(dv) == 0)
+    d = interior(du)
+    assert np.all(d == d[:, :1])
+    assert np.abs(d[1:M - 1]).min() > 0
+    ru, _ = weno_terms(o.get_state(), N, M)
+    assert np.max(np.abs(d - ru)) <= 1e-12 * np.max(np.abs(ru))
