@@ -41,6 +41,9 @@ constexpr int kRowChunk = 128;  // columns per chunk of a whole-row task
 #ifndef GDC_STRIP_BLOCKS
 #define GDC_STRIP_BLOCKS 2  // resident strip blocks per SM (FP32)
 #endif
+#ifndef GDC_STAGE_BLOCKS
+#define GDC_STAGE_BLOCKS 4  // resident stage blocks per SM the FP32 register budget targets
+#endif
 constexpr int kMaxKeep = 128;   // packed FFT coefficients a filter row may keep
 
 // ------------------------------------------------------------ helpers
@@ -198,8 +201,14 @@ struct Tile {
 };
 
 template <typename T, int R, int W>
-constexpr int tile_words() {
+GDC_HD constexpr int tile_words() {
   return 7 * Tile<T, R, W>::NS + kRecWords * Tile<T, R, W>::CR;
+}
+
+// Words of a whole-row task's staging tile, rounded to 16 bytes.
+template <typename T>
+GDC_HD constexpr int row_task_words() {
+  return (tile_words<T, 1, kRowChunk>() + 3) & ~3;
 }
 
 template <typename T, int R, int W>
@@ -238,7 +247,7 @@ __device__ __forceinline__ void cp_async16(T* smem, const T* gmem, bool valid) {
 // Requires num_lon and i0 to be multiples of VEC (checked at admission).
 template <typename T, int R, int W>
 __device__ void tile_issue(const MemberDev<T>& md, const T* __restrict__ gd, const T* __restrict__ iu,
-                           const T* __restrict__ iv, Tile<T, R, W>& t, bool given = false) {
+                           const T* __restrict__ iv, Tile<T, R, W>& t, bool given = false, bool want_ghs = true) {
   using TL = Tile<T, R, W>;
   constexpr int VEC = TL::VEC, NCH = W / VEC;
   const int N = md.N, M = md.M, Mh = md.Mh;
@@ -254,7 +263,7 @@ __device__ void tile_issue(const MemberDev<T>& md, const T* __restrict__ gd, con
     const size_t o = vf ? (size_t)j * N + t.i0 + k * VEC : 0;
     const int dp = TL::pos(rr, 1 + k * VEC);
     cp_async16(&t.gd[dp], gd + o, vf);
-    cp_async16(&t.ghs[dp], md.ghs + o, vf);
+    if (want_ghs) cp_async16(&t.ghs[dp], md.ghs + o, vf);
     cp_async16(&t.iu[dp], iu + o, vf);
     cp_async16(&t.iv[dp], iv + (vh ? o : 0), vh);
     if (given) {
@@ -274,7 +283,7 @@ __device__ void tile_issue(const MemberDev<T>& md, const T* __restrict__ gd, con
     const size_t o = vf ? (size_t)j * N + i : 0;
     const int dp = TL::pos(rr, cc);
     cp_async(&t.gd[dp], gd + o, vf);
-    cp_async(&t.ghs[dp], md.ghs + o, vf);
+    if (want_ghs) cp_async(&t.ghs[dp], md.ghs + o, vf);
     cp_async(&t.iu[dp], iu + o, vf);
     cp_async(&t.iv[dp], iv + (vh ? o : 0), vh);
     if (given) {
@@ -298,7 +307,7 @@ __device__ void tile_issue(const MemberDev<T>& md, const T* __restrict__ gd, con
 // j0-1..j0+R (local 0..R+1), columns i0-1..i0+W (local 0..W+1).
 template <typename T, int R, int W>
 __device__ void tile_derive(const MemberDev<T>& md, Tile<T, R, W>& t, bool u_halo_row = false,
-                            bool given = false) {
+                            bool given = false, bool want_v = true) {
   using TL = Tile<T, R, W>;
   const int M = md.M, Mh = md.Mh;
   cp_async_wait_all();
@@ -315,7 +324,7 @@ __device__ void tile_derive(const MemberDev<T>& md, Tile<T, R, W>& t, bool u_hal
     const bool need = rr <= t.vrows + 1 && cc <= t.vcols + 1;
     T uu = 0, vv = 0;
     if (need && rr >= urow0 && j >= 1 && j <= M - 2) uu = t.iu[p] * T(2) / (t.ig[p] + t.ig[p + 1]);
-    if (need && j >= 0 && j < Mh) vv = t.iv[p] * T(2) / (t.ig[p] + t.ig[p + TL::SW]);
+    if (want_v && need && j >= 0 && j < Mh) vv = t.iv[p] * T(2) / (t.ig[p] + t.ig[p + TL::SW]);
     t.u[p] = uu;
     t.v[p] = vv;
   }
@@ -779,7 +788,8 @@ __device__ __forceinline__ void bulk_tile(const MemberDev<T>& md, const StageArg
   static_assert(RPT * kThreads == R * W, "a tile is a whole number of rows per thread");
   const int N = md.N;
   TL t = carve<T, R, W>(staging, w.j0, w.i0, w.rows, w.cols);
-  tile_issue(md, gd_in, iu_in, iv_in, t, given);
+  // The slow pass (advection) reads no ghs, the fast pass no v.
+  tile_issue(md, gd_in, iu_in, iv_in, t, given, PASS != kSlowPass);
   const int c = threadIdx.x % W, r0 = (threadIdx.x / W) * RPT;
   const bool cval = c < w.cols;
   const int ob = (w.j0 + r0) * N + w.i0 + c;  // the thread's first point
@@ -793,7 +803,7 @@ __device__ __forceinline__ void bulk_tile(const MemberDev<T>& md, const StageArg
 #pragma unroll
       for (int f = 0; f < 3; ++f) pre[k][f] = (cval && r0 + k < w.rows) ? src[f][ob + k * N] : T(0);
   }
-  tile_derive(md, t, false, given);
+  tile_derive(md, t, false, given, PASS != kFastPass);
   T* dst[3] = {nullptr, nullptr, nullptr};
   T* tdst[3] = {nullptr, nullptr, nullptr};
 #pragma unroll
@@ -1197,7 +1207,7 @@ __device__ void row_tail(const MemberDev<T>& md, const StageArgs& a, Emit<T>& em
 
 template <typename T>
 struct StageOcc {
-  static constexpr int kMinBlocks = sizeof(T) == 4 ? 4 : 2;
+  static constexpr int kMinBlocks = sizeof(T) == 4 ? GDC_STAGE_BLOCKS : 2;
 };
 
 template <typename T, int PASS, int ADV, int R, int W>
@@ -1205,11 +1215,11 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
     stage_kernel(const MemberDev<T>* __restrict__ mems, const WorkItem* __restrict__ wl, StageArgs a,
                  int staging_words, int max_n) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* staging = reinterpret_cast<T*>(smem_raw);
-  T* rows = staging + staging_words;  // 3 * max_n (row tasks)
-  T* coefs = rows + 3 * max_n;        // kMaxKeep
-  T* redT = coefs + kMaxKeep;         // 64, then 64 doubles
-  T* tw = redT + 64 + 64 * (int)(sizeof(double) / sizeof(T));  // 2 * max_n twiddles
+  T* staging = reinterpret_cast<T*>(smem_raw);  // bulk tile, or the row task's tile, then:
+  T* rows = staging + row_task_words<T>();      // 3 * max_n (row tasks)
+  T* coefs = rows + 3 * max_n;                  // kMaxKeep
+  T* tw = coefs + kMaxKeep;                     // 2 * max_n twiddles
+  T* redT = staging + staging_words;            // 64, then 64 doubles
   __shared__ MemberDev<T> smd;
 
   const WorkItem w = wl[blockIdx.x];
@@ -1261,8 +1271,8 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
       const int vw = min(kRowChunk, N - c0);
       TR t = carve<T, 1, kRowChunk>(staging, j, c0, 1, vw);
       __syncthreads();
-      tile_issue(md, gd_in, iu_in, iv_in, t, given);
-      tile_derive(md, t, false, given);
+      tile_issue(md, gd_in, iu_in, iv_in, t, given, PASS != kSlowPass);
+      tile_derive(md, t, false, given, PASS != kFastPass);
       for (int c = threadIdx.x; c < vw; c += blockDim.x) {
         const int p = TR::pos(1, c + 1);
         const int i = c0 + c;
@@ -1639,12 +1649,14 @@ __global__ void __launch_bounds__(kThreads)
     diffusion_lap_kernel(const MemberDev<T>* __restrict__ mems, const WorkItem* __restrict__ wl, int slot, double c,
                          int staging_words, int max_n) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  // The stage kernel's layout (stage_smem_bytes): a bulk tile, or the row
+  // task's tile, rows, kept coefficients and twiddles, in one area.
   T* staging = reinterpret_cast<T*>(smem_raw);
-  T* rows = staging + staging_words;
+  T* rows = staging + row_task_words<T>();
   T* coefs = rows + 3 * max_n;
-  T* redT = coefs + kMaxKeep;
+  T* tw = coefs + kMaxKeep;  // 2 * max_n twiddles
+  T* redT = staging + staging_words;
   double* redD = reinterpret_cast<double*>(redT + 64);
-  T* tw = redT + 64 + 64 * (int)(sizeof(double) / sizeof(T));  // 2 * max_n twiddles
   __shared__ MemberDev<T> smd;
   const WorkItem w = wl[blockIdx.x];
   if (w.kind == 1 && w.field > 0) return;  // one block per whole row here (field -1 or F_GD)
@@ -1899,14 +1911,15 @@ size_t stage_smem_bytes(int tile_rows, int tile_cols, int max_n, int* staging_wo
   if (tile_rows == 8 && tile_cols == 64) bulk = tile_words<T, 8, 64>();
   if (tile_rows == 16 && tile_cols == 64) bulk = tile_words<T, 16, 64>();
   if (tile_rows == 4 && tile_cols == 128) bulk = tile_words<T, 4, 128>();
-  const int row = tile_words<T, 1, kRowChunk>();
+  // A block is a bulk tile or a whole-row task: the row task's tile, rows,
+  // kept coefficients and twiddles share the bulk tile's staging area.
   // Rounded to 4 words and max_n to an even count so that the FP64
-  // reduction buffer after the T arrays stays 8-byte aligned.
-  const int sw = ((bulk > row ? bulk : row) + 3) & ~3;
+  // reduction buffer after the area stays 8-byte aligned.
   max_n = (max_n + 1) & ~1;
+  const int row = row_task_words<T>() + 3 * max_n + kMaxKeep + 2 * max_n;
+  const int sw = ((bulk > row ? bulk : row) + 3) & ~3;
   if (staging_words) *staging_words = sw;
-  return (size_t)(sw + 3 * max_n + kMaxKeep + 64) * sizeof(T) + 64 * sizeof(double) + 2 * (size_t)max_n * sizeof(T) +
-         16;
+  return (size_t)(sw + 64) * sizeof(T) + 64 * sizeof(double) + 16;
 }
 
 template <typename T, int PASS, int ADV, int R, int W>
