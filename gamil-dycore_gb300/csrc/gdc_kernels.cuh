@@ -860,6 +860,164 @@ __device__ __forceinline__ void bulk_tile(const MemberDev<T>& md, const StageArg
   }
 }
 
+// ------------------------------------------------- column pairs (FP32)
+// FP32 bulk tiles may advance two adjacent columns per thread: each stencil
+// operand of the pair is one or two 8-byte shared loads instead of two
+// 4-byte ones, the results go out as 8-byte stores, and the point
+// operators run on F2 (component-wise float arithmetic, contracted to FMA
+// as the scalar path is).  The values are the scalar path's.
+#ifndef GDC_PAIR
+#define GDC_PAIR 1
+#endif
+
+struct F2 {
+  float x, y;
+  F2() = default;
+  __device__ __forceinline__ F2(float a) : x(a), y(a) {}
+  __device__ __forceinline__ F2(float a, float b) : x(a), y(b) {}
+  __device__ __forceinline__ explicit F2(double a) : x((float)a), y((float)a) {}
+  __device__ __forceinline__ F2(int a) : x((float)a), y((float)a) {}
+};
+__device__ __forceinline__ F2 operator+(F2 a, F2 b) { return F2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ F2 operator-(F2 a, F2 b) { return F2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ F2 operator*(F2 a, F2 b) { return F2(a.x * b.x, a.y * b.y); }
+__device__ __forceinline__ F2 operator/(F2 a, F2 b) { return F2(a.x / b.x, a.y / b.y); }
+__device__ __forceinline__ F2 operator-(F2 a) { return F2(-a.x, -a.y); }
+__device__ __forceinline__ F2 fabs(F2 a) { return F2(fabsf(a.x), fabsf(a.y)); }
+__device__ __forceinline__ F2 ld2(const float* p) {
+  const float2 v = *reinterpret_cast<const float2*>(p);
+  return F2(v.x, v.y);
+}
+__device__ __forceinline__ void st2(float* p, F2 v) { *reinterpret_cast<float2*>(p) = make_float2(v.x, v.y); }
+
+// Stencil view of a column pair: p is the (even) tile position of its
+// first column; offsets dc = -1, 0, 1 come from the aligned pairs at
+// p - 2, p, p + 2.
+template <class TL>
+struct TileView2 {
+  const TL& t;
+  int p, j;
+  __device__ __forceinline__ F2 at(const float* a, int dr, int dc) const {
+    const float* b = a + p + dr * TL::SW;
+    const F2 c = ld2(b);
+    if (dc == 0) return c;
+    if (dc < 0) return F2(ld2(b - 2).y, c.x);
+    return F2(c.y, ld2(b + 2).x);
+  }
+  __device__ __forceinline__ F2 u(int dr, int dc) const { return at(t.u, dr, dc); }
+  __device__ __forceinline__ F2 v(int dr, int dc) const { return at(t.v, dr, dc); }
+  __device__ __forceinline__ F2 iu(int dr, int dc) const { return at(t.iu, dr, dc); }
+  __device__ __forceinline__ F2 iv(int dr, int dc) const { return at(t.iv, dr, dc); }
+  __device__ __forceinline__ F2 ig(int dr, int dc) const { return at(t.ig, dr, dc); }
+  __device__ __forceinline__ F2 gd(int dr, int dc) const { return at(t.gd, dr, dc); }
+  __device__ __forceinline__ F2 ghs(int dr, int dc) const { return at(t.ghs, dr, dc); }
+  __device__ __forceinline__ float cf(int k, int jj) const { return t.cf(k, jj); }
+  __device__ __forceinline__ float ch(int k, int jj) const { return t.ch(k, jj); }
+};
+
+// bulk_tile for FP32 with column pairs: thread t owns columns c, c+1
+// (c = 2 (t % (W/2))) of RPT consecutive rows.  Tile columns are even in
+// number (num_lon and i0 are multiples of 4), so a pair never straddles a
+// partial tile's edge.
+template <int PASS, int ADV, int R, int W, int UF>
+__device__ __forceinline__ void bulk_tile_pair(const MemberDev<float>& md, const StageArgs& a, const WorkItem& w,
+                                               float* staging, bool given, const float* gd_in, const float* iu_in,
+                                               const float* iv_in, float ub_lon, float ub_lat, Emit<float>& em) {
+  using T = float;
+  using TL = Tile<T, R, W>;
+  constexpr int PW = W / 2, RPT = R * PW / kThreads;
+  static_assert(RPT * kThreads == R * PW, "a tile is a whole number of pair rows per thread");
+  const int N = md.N;
+  TL t = carve<T, R, W>(staging, w.j0, w.i0, w.rows, w.cols);
+  tile_issue(md, gd_in, iu_in, iv_in, t, given, PASS != kSlowPass);
+  const int c = 2 * (threadIdx.x % PW), r0 = (threadIdx.x / PW) * RPT;
+  const bool cval = c < w.cols;
+  const int ob = (w.j0 + r0) * N + w.i0 + c;
+  F2 pre[RPT][3];
+  if (UF == UF_PREDICT_OUT || UF == UF_CORRECT) {
+    T* const* src = UF == UF_PREDICT_OUT ? md.st[a.base_slot] : md.td[a.tprev];
+#pragma unroll
+    for (int k = 0; k < RPT; ++k)
+#pragma unroll
+      for (int f = 0; f < 3; ++f) pre[k][f] = (cval && r0 + k < w.rows) ? ld2(src[f] + ob + k * N) : F2(0.0f);
+  }
+  tile_derive(md, t, false, given, PASS != kFastPass);
+  T* dst[3] = {nullptr, nullptr, nullptr};
+  T* tdst[3] = {nullptr, nullptr, nullptr};
+#pragma unroll
+  for (int f = 0; f < 3; ++f) {
+    if (UF == UF_PREDICT_IN || UF == UF_PREDICT_OUT) dst[f] = md.st[a.out_slot][f];
+    if (UF == UF_PREDICT_OUT || UF == UF_CORRECT) tdst[f] = md.td[a.tout][f];
+  }
+  const F2 h(em.h);
+#pragma unroll
+  for (int k = 0; k < RPT; ++k) {
+    const int r = r0 + k;
+    if (!cval || r >= w.rows) continue;
+    const int j = w.j0 + r, o = ob + k * N;
+    const int p = TL::pos(r + 1, c + 1);
+    const TileView2<TL> sv{t, p, j};
+    F2 wu(0.0f), wv(0.0f);
+    if (ADV == GDC_ADV_WENO && PASS != kFastPass) {
+      wu = ld2(md.wadv[0] + o);
+      wv = ld2(md.wadv[1] + o);
+    }
+    const F2 du = point_du<F2, PASS, ADV>(sv, F2(ub_lon), F2(ub_lat), wu);
+    const F2 dv = point_dv<F2, PASS, ADV>(sv, F2(ub_lon), F2(ub_lat), wv);
+    const F2 dg = point_dgd<F2, PASS>(sv);
+    if (UF == UF_PREDICT_IN) {
+      st2(dst[F_IU] + o, ld2(t.iu + p) + h * du);
+      st2(dst[F_IV] + o, ld2(t.iv + p) + h * dv);
+      st2(dst[F_GD] + o, ld2(t.gd + p) + h * dg);
+    } else if (UF == UF_PREDICT_OUT) {
+      st2(tdst[F_IU] + o, du);
+      st2(dst[F_IU] + o, pre[k][F_IU] + h * du);
+      st2(tdst[F_IV] + o, dv);
+      st2(dst[F_IV] + o, pre[k][F_IV] + h * dv);
+      st2(tdst[F_GD] + o, dg);
+      st2(dst[F_GD] + o, pre[k][F_GD] + h * dg);
+    } else if (UF == UF_CORRECT) {
+      const T wf = t.cf(TF_COS, j), wh = t.ch(TH_COS, j);
+      st2(tdst[F_IU] + o, du);
+      st2(tdst[F_IV] + o, dv);
+      st2(tdst[F_GD] + o, dg);
+      // the scalar path's order of terms, point by point
+      em.ip1.add(pre[k][F_IU].x * du.x * wf);
+      em.ip2.add(du.x * du.x * wf);
+      em.ip1.add(pre[k][F_IV].x * dv.x * wh);
+      em.ip2.add(dv.x * dv.x * wh);
+      em.ip1.add(pre[k][F_GD].x * dg.x * wf);
+      em.ip2.add(dg.x * dg.x * wf);
+      em.ip1.add(pre[k][F_IU].y * du.y * wf);
+      em.ip2.add(du.y * du.y * wf);
+      em.ip1.add(pre[k][F_IV].y * dv.y * wh);
+      em.ip2.add(dv.y * dv.y * wh);
+      em.ip1.add(pre[k][F_GD].y * dg.y * wf);
+      em.ip2.add(dg.y * dg.y * wf);
+    } else {
+      const T wf = t.cf(TF_COS, j), wh = t.ch(TH_COS, j);
+      em.put(F_IU, o, du.x, wf, em.base_of(F_IU, o), em.prev_of(F_IU, o));
+      em.put(F_IV, o, dv.x, wh, em.base_of(F_IV, o), em.prev_of(F_IV, o));
+      em.put(F_GD, o, dg.x, wf, em.base_of(F_GD, o), em.prev_of(F_GD, o));
+      em.put(F_IU, o + 1, du.y, wf, em.base_of(F_IU, o + 1), em.prev_of(F_IU, o + 1));
+      em.put(F_IV, o + 1, dv.y, wh, em.base_of(F_IV, o + 1), em.prev_of(F_IV, o + 1));
+      em.put(F_GD, o + 1, dg.y, wf, em.base_of(F_GD, o + 1), em.prev_of(F_GD, o + 1));
+    }
+  }
+}
+
+// The bulk tile of a stage: column pairs for FP32 tiles whose pair count
+// divides evenly among the threads, else one column per thread.
+template <typename T, int PASS, int ADV, int R, int W, int UF>
+__device__ __forceinline__ void bulk_tile_any(const MemberDev<T>& md, const StageArgs& a, const WorkItem& w,
+                                              T* staging, bool given, const T* gd_in, const T* iu_in,
+                                              const T* iv_in, T ub_lon, T ub_lat, Emit<T>& em) {
+  if constexpr (GDC_PAIR && sizeof(T) == 4 && (R * W / 2) % kThreads == 0)
+    bulk_tile_pair<PASS, ADV, R, W, UF>(md, a, w, staging, given, gd_in, iu_in, iv_in, ub_lon, ub_lat, em);
+  else
+    bulk_tile<T, PASS, ADV, R, W, UF>(md, a, w, staging, given, gd_in, iu_in, iv_in, ub_lon, ub_lat, em);
+}
+
 // ------------------------------------------------------------ warp strips
 // One warp advances one strip: output columns i0..i0+cols-1 (cols <= 30) of
 // rows j0..j0+rows-1, all ordinary.  Lane L holds column i0-1+L (mod N) of
@@ -1241,7 +1399,7 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
   if (w.kind == 0) {
     // ---------------- bulk tile: rows j0..j0+R-1 are ordinary rows
 #define GDC_BULK(F)                                                                                   \
-  bulk_tile<T, PASS, ADV, R, W, F>(md, a, w, staging, given, gd_in, iu_in, iv_in, ub_lon, ub_lat, em); \
+  bulk_tile_any<T, PASS, ADV, R, W, F>(md, a, w, staging, given, gd_in, iu_in, iv_in, ub_lon, ub_lat, em); \
   break;
     switch (a.form) {
       case UF_PREDICT_IN:
