@@ -310,13 +310,33 @@ __device__ void tile_derive(const MemberDev<T>& md, Tile<T, R, W>& t, bool u_hal
                             bool given = false, bool want_v = true) {
   using TL = Tile<T, R, W>;
   const int M = md.M, Mh = md.Mh;
+  const int urow0 = u_halo_row ? 0 : 1;
+  constexpr int DW = W + 2, ND = (R + 2) * (W + 2);
   cp_async_wait_all();
   __syncthreads();
+  if constexpr (sizeof(T) == 4) {
+    // FP32: one pass and one barrier fewer -- each position takes the
+    // square roots it divides by itself (the same values as ig).
+    for (int q = threadIdx.x; q < ND; q += kThreads) {
+      const int rr = q / DW, cc = q - rr * DW;
+      const int p = TL::pos(rr, cc);
+      if (rr > t.vrows + 1 || cc > t.vcols + 1) continue;
+      const int j = t.j0 - 1 + rr;
+      const T g0 = sqrt(t.gd[p]);
+      t.ig[p] = g0;
+      if (given) continue;
+      T uu = 0, vv = 0;
+      if (rr >= urow0 && j >= 1 && j <= M - 2) uu = t.iu[p] * T(2) / (g0 + sqrt(t.gd[p + 1]));
+      if (want_v && j >= 0 && j < Mh) vv = t.iv[p] * T(2) / (g0 + sqrt(t.gd[p + TL::SW]));
+      t.u[p] = uu;
+      t.v[p] = vv;
+    }
+    __syncthreads();
+    return;
+  }
   for (int p = threadIdx.x; p < TL::NS; p += kThreads) t.ig[p] = sqrt(t.gd[p]);
   __syncthreads();
   if (given) return;
-  const int urow0 = u_halo_row ? 0 : 1;
-  constexpr int DW = W + 2, ND = (R + 2) * (W + 2);
   for (int q = threadIdx.x; q < ND; q += kThreads) {
     const int rr = q / DW, cc = q - rr * DW;
     const int p = TL::pos(rr, cc);
