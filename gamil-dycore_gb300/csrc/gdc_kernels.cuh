@@ -1527,14 +1527,14 @@ __global__ void __launch_bounds__(kThreads, StripOcc<T>::kMinBlocks)
 
 // beta of predict_correct (src/dycore_mod.F90:784-786) or isp (:743-746),
 // one block per member over that member's partials.
+// beta of member slot s from its md.pcount partials (src/dycore_mod.F90:
+// 784-787; isp :743-747), reduced by the whole block in a fixed order.
+// FP64: double-double (the oracle's correctly rounded sums); FP32: the
+// partials carry FP32 rounding, a plain FP64 sum loses nothing.
 template <typename T>
-__global__ void __launch_bounds__(kThreads)
-    beta_kernel(const MemberDev<T>* __restrict__ mems, const int* __restrict__ slots, const double* partials,
-                double* beta, int qcon, int beta_mode) {
-  __shared__ double red[64];
-  const int s = slots[blockIdx.x];
-  const MemberDev<T>& md = mems[s];
-  Acc<double> a1, a2;
+__device__ void member_beta(const MemberDev<T>& md, int s, const double* partials, double* beta, int qcon,
+                            int beta_mode, double* red) {
+  typename DiagAcc<T>::type a1, a2;
   for (int q = threadIdx.x; q < md.pcount; q += blockDim.x) {
     const double* pp = partials + 4 * (size_t)(md.pbase + q);
     a1.merge(pp[0], pp[1]);
@@ -1547,6 +1547,15 @@ __global__ void __launch_bounds__(kThreads)
     if (beta_mode == 1) b = b * 4.0 / md.dt;
     beta[s] = b;
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    beta_kernel(const MemberDev<T>* __restrict__ mems, const int* __restrict__ slots, const double* partials,
+                double* beta, int qcon, int beta_mode) {
+  __shared__ double red[64];
+  const int s = slots[blockIdx.x];
+  member_beta<T>(mems[s], s, partials, beta, qcon, beta_mode, red);
 }
 
 // ------------------------------------------------------ final update

@@ -88,6 +88,32 @@ def test_every_tile_shape_matches_oracle_on_ragged_grid(native, tile):
         assert np.array_equal(interior(a), interior(ref[name])), (tile, name)
 
 
+@pytest.mark.parametrize("tile", [(8, 32), (8, 64), (4, 128), (16, 64)])
+def test_every_fp32_tile_shape_near_oracle_on_ragged_grid(native, tile):
+    """The FP32 kernels (column pairs where the tile allows) under every tile
+    shape: one step within 1e-5 (relative L2) of the FP64 oracle, on the
+    serving scheme of this grid (8 subcycles, 10 filtered rows: the gravity
+    waves of the first unfiltered row are within their CFL limit)."""
+    from oracle.oracle import OracleModel
+    N, M = 720, 361
+    p = scheme(gdc, N, M, 120.0, subcycles=8, cutoff=(4,) * 10, precision=gdc.FP32)
+    p.filter_rescale_rtol = 1e-5
+    ic = gdc.ic_seeded(N, M, seed=5)
+    b = gdc.Batch(p)
+    b.set_tile(*tile)
+    mid = b.add(N, M, 120.0, 1, *ic)
+    b.step(1)
+    b.sync()
+    got = b.get_state(mid)
+    b.close()
+    o = OracleModel.from_params(p)
+    o.set_state(*ic)
+    o.step(1)
+    ref = o.get_state()
+    for name, a in zip(("u", "v", "gd"), got):
+        assert rel_l2(a, ref[name]) < 1e-5, (tile, name, rel_l2(a, ref[name]))
+
+
 @pytest.mark.parametrize("shape", [(8, 30), (16, 30), (32, 30), (64, 30)])
 @pytest.mark.parametrize("N,M", [(720, 361), (200, 101)])
 def test_warp_strips_match_oracle(native, shape, N, M):
