@@ -355,46 +355,47 @@ class Batch final : public BatchIface {
     MemberRec& r = recs[slot];
     const MemberDev<T>& d = hdesc[slot];
     const int Mh = M - 1;
-    // iap_transform of the initial condition (src/types_mod.F90:399-426) in
-    // FP64 on the host, exactly as the reference evaluates it.
-    const size_t full = (size_t)M * N, half = (size_t)Mh * N;
-    std::vector<double> hg(full), hu(full), hv(half), hghs(full);
-    auto at = [&](const double* f, int i, int j) { return f[(size_t)(j + 2) * ld + (i + 2)]; };
-    std::vector<double> ig(full);
-    for (int j = 0; j < M; ++j)
-      for (int i = 0; i < N; ++i) {
-        hg[(size_t)j * N + i] = at(gd, i, j);
-        hghs[(size_t)j * N + i] = at(ghs, i, j);
-        ig[(size_t)j * N + i] = std::sqrt(at(gd, i, j));
-      }
-    for (int j = 0; j < M; ++j)
-      for (int i = 0; i < N; ++i) {
-        const int ip = (i + 1) % N;
-        hu[(size_t)j * N + i] = 0.5 * (ig[(size_t)j * N + i] + ig[(size_t)j * N + ip]) * at(u, i, j);
-      }
-    for (int j = 0; j < Mh; ++j)
-      for (int i = 0; i < N; ++i)
-        hv[(size_t)j * N + i] = 0.5 * (ig[(size_t)j * N + i] + ig[(size_t)(j + 1) * N + i]) * at(v, i, j);
+    // The initial condition goes up as it is (FP64, compact rows: u, v, gd,
+    // ghs); its iap_transform (src/types_mod.F90:399-426) runs on the device
+    // in FP64 with the reference's operations and rounding (ic_iap_kernel),
+    // and its own u, v become the level's given u, v: the first stage reads
+    // them as given (state(1)%u, %v in the reference), not re-derived.
+    const size_t full = (size_t)M * N, half = (size_t)Mh * N, words = 3 * full + half;
     r.ic_ld = ld;
     r.ic_u.assign(u, u + (size_t)ld * (M + 4));
     r.ic_v.assign(v, v + (size_t)ld * (Mh + 4));
-    cudaError_t e = upload_field(d.ghs, nullptr, hghs);
-    const int lvl = old_;
-    if (e == cudaSuccess) e = upload_field(d.st[lvl][F_GD], d.lo[lvl][F_GD], hg);
-    if (e == cudaSuccess) e = upload_field(d.st[lvl][F_IU], d.lo[lvl][F_IU], hu);
-    if (e == cudaSuccess) e = upload_field(d.st[lvl][F_IV], d.lo[lvl][F_IV], hv);
-    {
-      // The initial condition's own u, v: the first stage reads them as
-      // given (state(1)%u, %v in the reference), not re-derived.
-      std::vector<double> gu(full), gv(half);
-      for (int j = 0; j < M; ++j)
-        for (int i = 0; i < N; ++i) gu[(size_t)j * N + i] = at(u, i, j);
-      for (int j = 0; j < Mh; ++j)
-        for (int i = 0; i < N; ++i) gv[(size_t)j * N + i] = at(v, i, j);
-      if (e == cudaSuccess) e = upload_field(d.given_u, nullptr, gu);
-      if (e == cudaSuccess) e = upload_field(d.given_v, nullptr, gv);
-      if (e == cudaSuccess) e = cudaMemcpy(d_uvslot + slot, &lvl, sizeof(int), cudaMemcpyHostToDevice);
+    if (h_ic.size() < words) h_ic.resize(words);
+    double* hu = h_ic.data();
+    double* hv = hu + full;
+    double* hg = hv + half;
+    double* hh = hg + full;
+    for (int j = 0; j < M; ++j) {
+      const size_t src = (size_t)(j + 2) * ld + 2, dst = (size_t)j * N;
+      std::memcpy(hu + dst, u + src, N * sizeof(double));
+      std::memcpy(hg + dst, gd + src, N * sizeof(double));
+      std::memcpy(hh + dst, ghs + src, N * sizeof(double));
+      if (j < Mh) std::memcpy(hv + dst, v + src, N * sizeof(double));
     }
+    cudaError_t e = cudaSuccess;
+    if (ictmp_cap < words) {
+      if (d_ictmp) cudaFree(d_ictmp);
+      d_ictmp = nullptr;
+      ictmp_cap = 0;
+      e = cudaMalloc(&d_ictmp, words * sizeof(double));
+      if (e == cudaSuccess) ictmp_cap = words;
+    }
+    const int lvl = old_;
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_ictmp, hu, words * sizeof(double), cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) {
+      double* du = d_ictmp;
+      double* dv = du + full;
+      double* dg = dv + half;
+      if (launch_ic_iap<T>(d_mem, slot, lvl, N, M, du, dv, dg, dg + full, stream) != GDC_OK)
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_uvslot + slot, &lvl, sizeof(int), cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) {
       release(slot);
       return fail(GDC_E_CUDA, cuda_msg("add: upload", e));
@@ -1014,6 +1015,9 @@ class Batch final : public BatchIface {
   int* d_active = nullptr;  // slots of the active members (beta / diag blocks)
   int* d_uvslot = nullptr;  // per member: level whose u, v are held as given (-1 none)
   double* d_beta = nullptr;
+  double* d_ictmp = nullptr;  // an admitted initial condition in FP64 (grow-only)
+  size_t ictmp_cap = 0;       // its capacity in doubles
+  std::vector<double> h_ic;   // host staging of the same
   double* d_diag = nullptr;
   long long* d_steps = nullptr;
   long long* d_nan = nullptr;
@@ -1113,22 +1117,11 @@ class Batch final : public BatchIface {
     if (d_dl) cudaFree(d_dl);
     if (d_dpart) cudaFree(d_dpart);
     if (d_partials) cudaFree(d_partials);
+    if (d_ictmp) cudaFree(d_ictmp);
     if (own_stream) cudaStreamDestroy(own_stream);
     if (side) cudaStreamDestroy(side);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
-  }
-
-  cudaError_t upload_field(T* dst, T* lo, const std::vector<double>& src) {
-    std::vector<T> hi(src.size()), lw;
-    if (lo) lw.resize(src.size());
-    for (size_t q = 0; q < src.size(); ++q) {
-      hi[q] = T(src[q]);
-      if (lo) lw[q] = T(src[q] - (double)hi[q]);
-    }
-    cudaError_t e = cudaMemcpy(dst, hi.data(), hi.size() * sizeof(T), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && lo) e = cudaMemcpy(lo, lw.data(), lw.size() * sizeof(T), cudaMemcpyHostToDevice);
-    return e;
   }
 
   cudaError_t download_field(const T* src, const T* lo, size_t n, std::vector<double>& out) {
