@@ -376,14 +376,7 @@ class Batch final : public BatchIface {
       std::memcpy(hh + dst, ghs + src, N * sizeof(double));
       if (j < Mh) std::memcpy(hv + dst, v + src, N * sizeof(double));
     }
-    cudaError_t e = cudaSuccess;
-    if (ictmp_cap < words) {
-      if (d_ictmp) cudaFree(d_ictmp);
-      d_ictmp = nullptr;
-      ictmp_cap = 0;
-      e = cudaMalloc(&d_ictmp, words * sizeof(double));
-      if (e == cudaSuccess) ictmp_cap = words;
-    }
+    cudaError_t e = ensure_tmp(words);
     const int lvl = old_;
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(d_ictmp, hu, words * sizeof(double), cudaMemcpyHostToDevice, stream);
@@ -759,19 +752,32 @@ class Batch final : public BatchIface {
     sync_stream();
     // state(old) of this member: its last written level.
     const int lvl = level_of(id);
-    const MemberDev<T>& d = hdesc[id];
-    std::vector<double> hg, hu, hv;
-    cudaError_t e = download_field(d.st[lvl][F_GD], d.lo[lvl][F_GD], (size_t)M * N, hg);
-    if (e == cudaSuccess) e = download_field(d.st[lvl][F_IU], d.lo[lvl][F_IU], (size_t)M * N, hu);
-    if (e == cudaSuccess) e = download_field(d.st[lvl][F_IV], d.lo[lvl][F_IV], (size_t)Mh * N, hv);
+    int uvs = -1;
+    cudaError_t e = cudaMemcpy(&uvs, d_uvslot + id, sizeof(int), cudaMemcpyDeviceToHost);
+    const bool ic_uv = r.steps_done == 0 && std::is_same<T, double>::value && !r.ic_u.empty();
+    const int uv_mode = (ic_uv || !(u || v)) ? 2 : (uvs == lvl ? 1 : 0);
+    // The level in FP64 on the device (hi + lo, square roots, u and v as
+    // update_state recovers them, src/dycore_mod.F90:636-645), one copy back.
+    const size_t n = (size_t)M * N, nh = (size_t)Mh * N, words = 4 * n + 2 * nh;
+    if (e == cudaSuccess) e = ensure_tmp(words);
+    if (e == cudaSuccess && launch_state_out<T>(d_mem, id, lvl, uv_mode, N, M, d_ictmp, stream) != GDC_OK)
+      e = cudaGetLastError();
+    if (h_ic.size() < words) h_ic.resize(words);
+    // gd, u, v first: the usual request copies only those
+    const size_t back = (iu || iv || ig) ? words : 2 * n + nh;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_ic.data(), d_ictmp, back * sizeof(double), cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("get_state", e));
-    std::vector<double> sg((size_t)M * N);
-    for (size_t q = 0; q < sg.size(); ++q) sg[q] = std::sqrt(hg[q]);
-    auto put = [&](double* f, int rows, auto value) {
+    const double* hg = h_ic.data();
+    const double* ou = hg + n;
+    const double* ov = ou + n;
+    const double* hu = ov + nh;
+    const double* hv = hu + n;
+    const double* sg = hv + nh;
+    auto put = [&](double* f, int rows, const double* src) {
       if (!f) return;
       std::memset(f, 0, sizeof(double) * (size_t)ld * (rows + 4));
-      for (int j = 0; j < rows; ++j)
-        for (int i = 0; i < N; ++i) f[(size_t)(j + 2) * ld + i + 2] = value(i, j);
+      for (int j = 0; j < rows; ++j) std::memcpy(f + (size_t)(j + 2) * ld + 2, src + (size_t)j * N, N * sizeof(double));
       for (int j = 0; j < rows + 4; ++j) {
         double* row = f + (size_t)j * ld;
         row[0] = row[N];
@@ -780,13 +786,11 @@ class Batch final : public BatchIface {
         row[N + 3] = row[3];
       }
     };
-    put(gd, M, [&](int i, int j) { return hg[(size_t)j * N + i]; });
-    put(iu, M, [&](int i, int j) { return hu[(size_t)j * N + i]; });
-    put(iv, Mh, [&](int i, int j) { return hv[(size_t)j * N + i]; });
-    put(ig, M, [&](int i, int j) { return sg[(size_t)j * N + i]; });
-    int uvs = -1;
-    cudaMemcpy(&uvs, d_uvslot + id, sizeof(int), cudaMemcpyDeviceToHost);
-    if (r.steps_done == 0 && std::is_same<T, double>::value && !r.ic_u.empty()) {
+    put(gd, M, hg);
+    put(iu, M, hu);
+    put(iv, Mh, hv);
+    put(ig, M, sg);
+    if (ic_uv) {
       // state(old) still holds the initial condition's own u and v.
       auto copy_ic = [&](double* f, const std::vector<double>& src, int rows) {
         if (!f) return;
@@ -795,24 +799,9 @@ class Batch final : public BatchIface {
       };
       copy_ic(u, r.ic_u, M);
       copy_ic(v, r.ic_v, Mh);
-    } else if (uvs == lvl && (u || v)) {
-      // u, v held as given with this level (after diffusion).
-      std::vector<double> gu, gv;
-      e = download_field(d.given_u, nullptr, (size_t)M * N, gu);
-      if (e == cudaSuccess) e = download_field(d.given_v, nullptr, (size_t)Mh * N, gv);
-      if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("get_state: u, v", e));
-      put(u, M, [&](int i, int j) { return gu[(size_t)j * N + i]; });
-      put(v, Mh, [&](int i, int j) { return gv[(size_t)j * N + i]; });
-    } else {
-      // update_state's recovery of u and v (src/dycore_mod.F90:636-645).
-      put(u, M, [&](int i, int j) {
-        if (j == 0 || j == M - 1) return 0.0;
-        const int ip = (i + 1) % N;
-        return hu[(size_t)j * N + i] * 2.0 / (sg[(size_t)j * N + i] + sg[(size_t)j * N + ip]);
-      });
-      put(v, Mh, [&](int i, int j) {
-        return hv[(size_t)j * N + i] * 2.0 / (sg[(size_t)j * N + i] + sg[(size_t)(j + 1) * N + i]);
-      });
+    } else if (uv_mode != 2) {
+      put(u, M, ou);
+      put(v, Mh, ov);
     }
     return GDC_OK;
   }
@@ -1015,7 +1004,7 @@ class Batch final : public BatchIface {
   int* d_active = nullptr;  // slots of the active members (beta / diag blocks)
   int* d_uvslot = nullptr;  // per member: level whose u, v are held as given (-1 none)
   double* d_beta = nullptr;
-  double* d_ictmp = nullptr;  // an admitted initial condition in FP64 (grow-only)
+  double* d_ictmp = nullptr;  // FP64 scratch: an admitted initial condition, a read-back level
   size_t ictmp_cap = 0;       // its capacity in doubles
   std::vector<double> h_ic;   // host staging of the same
   double* d_diag = nullptr;
@@ -1122,6 +1111,20 @@ class Batch final : public BatchIface {
     if (side) cudaStreamDestroy(side);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
+  }
+
+  // The FP64 scratch for admissions and read-backs, grown on demand.
+  cudaError_t ensure_tmp(size_t words) {
+    if (ictmp_cap >= words) return cudaSuccess;
+    if (d_ictmp) cudaFree(d_ictmp);
+    d_ictmp = nullptr;
+    ictmp_cap = 0;
+    cudaError_t e = cudaMalloc(&d_ictmp, words * sizeof(double));
+    if (e == cudaSuccess)
+      ictmp_cap = words;
+    else
+      cudaGetLastError();
+    return e;
   }
 
   cudaError_t download_field(const T* src, const T* lo, size_t n, std::vector<double>& out) {

@@ -336,6 +336,12 @@ int launch_stage_strips(const MemberDev<T>* mem, const WorkItem* strips, int nst
 template <typename T>
 int launch_ic_iap(const MemberDev<T>* mem, int slot, int lvl, int N, int M, const double* u, const double* v,
                   const double* gd, const double* ghs, void* stream);
+// Member `slot`'s level `lvl` in FP64, compact: gd [M N], u [M N],
+// v [Mh N], iap u [M N], iap v [Mh N], iap gd [M N]; u, v derived
+// (uv_mode 0), the given ones (1) or not written (2).
+template <typename T>
+int launch_state_out(const MemberDev<T>* mem, int slot, int lvl, int uv_mode, int N, int M, double* out,
+                     void* stream);
 // The WENO advection terms of every member's level `in_slot` (flat items
 // of the iap u and v fields; gd items are skipped).
 template <typename T>

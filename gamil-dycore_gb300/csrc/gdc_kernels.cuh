@@ -29,6 +29,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 
@@ -2238,6 +2239,56 @@ int launch_ic_iap(const MemberDev<T>* mem, int slot, int lvl, int N, int M, cons
                   const double* gd, const double* ghs, void* stream) {
   const int n = N * M, grid = (n + kThreads - 1) / kThreads;
   ic_iap_kernel<T><<<grid, kThreads, 0, (cudaStream_t)stream>>>(mem, slot, lvl, u, v, gd, ghs);
+  return check_launch();
+}
+
+// A member's level `lvl` read back in FP64 (hi + lo), compact: gd, u, v,
+// iap u, iap v, iap gd (sqrt gd) -- u, v derived as update_state recovers them
+// (src/dycore_mod.F90:636-645; zero on the pole rows) with uv_mode 0, the
+// level's given u, v with 1, not written with 2.  Explicitly rounded FP64
+// operations: the same values as the same arithmetic on the host.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    state_out_kernel(const MemberDev<T>* __restrict__ mems, int slot, int lvl, int uv_mode, double* __restrict__ out) {
+  const MemberDev<T>& d = mems[slot];
+  const int N = d.N, M = d.M, Mh = d.Mh;
+  const size_t n = (size_t)M * N, nh = (size_t)Mh * N;
+  double* og = out;
+  double* ouu = og + n;
+  double* ovv = ouu + n;
+  double* ou = ovv + nh;
+  double* ov = ou + n;
+  double* oi = ov + nh;
+  const T *gh = d.st[lvl][F_GD], *gl = d.lo[lvl][F_GD];
+  auto level = [](const T* hi, const T* lo, size_t q) {
+    return __dadd_rn((double)hi[q], lo ? (double)lo[q] : 0.0);
+  };
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(q / N), i = (int)(q - (size_t)j * N);
+    const double g = level(gh, gl, q), sg = __dsqrt_rn(g);
+    const double iu = level(d.st[lvl][F_IU], d.lo[lvl][F_IU], q);
+    og[q] = g;
+    ou[q] = iu;
+    oi[q] = sg;
+    if (j < Mh) ov[q] = level(d.st[lvl][F_IV], d.lo[lvl][F_IV], q);
+    if (uv_mode == 1) {
+      ouu[q] = __dadd_rn((double)d.given_u[q], 0.0);
+      if (j < Mh) ovv[q] = __dadd_rn((double)d.given_v[q], 0.0);
+    } else if (uv_mode == 0) {
+      const size_t qp = i + 1 == N ? q + 1 - N : q + 1;
+      ouu[q] = (j == 0 || j == M - 1) ? 0.0
+                                      : __ddiv_rn(__dmul_rn(iu, 2.0), __dadd_rn(sg, __dsqrt_rn(level(gh, gl, qp))));
+      if (j < Mh)
+        ovv[q] = __ddiv_rn(__dmul_rn(ov[q], 2.0), __dadd_rn(sg, __dsqrt_rn(level(gh, gl, q + N))));
+    }
+  }
+}
+
+template <typename T>
+int launch_state_out(const MemberDev<T>* mem, int slot, int lvl, int uv_mode, int N, int M, double* out,
+                     void* stream) {
+  const int grid = (int)std::min<size_t>(((size_t)N * M + kThreads - 1) / kThreads, 4096);
+  state_out_kernel<T><<<grid, kThreads, 0, (cudaStream_t)stream>>>(mem, slot, lvl, uv_mode, out);
   return check_launch();
 }
 

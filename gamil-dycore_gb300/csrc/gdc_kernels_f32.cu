@@ -15,6 +15,7 @@ template int launch_history<float>(const MemberDev<float>*, int, int, int, int, 
 template int launch_ic_iap<float>(const MemberDev<float>*, int, int, int, int, const double*, const double*,
                                  const double*, const double*, void*);
 template int launch_weno<float>(const MemberDev<float>*, const FlatItem*, int, int, const int*, void*);
+template int launch_state_out<float>(const MemberDev<float>*, int, int, int, int, int, double*, void*);
 template int launch_final<float>(const MemberDev<float>*, const FlatItem*, int, const FinalArgs&, void*);
 template int launch_diag<float>(const MemberDev<float>*, const FlatItem*, int, const int*, int, const DiagArgs&, void*);
 template int launch_beta<float>(const MemberDev<float>*, const int*, int, const double*, double*, int, int, void*);

@@ -18,6 +18,7 @@ template int launch_history<double>(const MemberDev<double>*, int, int, int, int
 template int launch_ic_iap<double>(const MemberDev<double>*, int, int, int, int, const double*, const double*,
                                  const double*, const double*, void*);
 template int launch_weno<double>(const MemberDev<double>*, const FlatItem*, int, int, const int*, void*);
+template int launch_state_out<double>(const MemberDev<double>*, int, int, int, int, int, double*, void*);
 template int launch_final<double>(const MemberDev<double>*, const FlatItem*, int, const FinalArgs&, void*);
 template int launch_diag<double>(const MemberDev<double>*, const FlatItem*, int, const int*, int, const DiagArgs&, void*);
 template int launch_beta<double>(const MemberDev<double>*, const int*, int, const double*, double*, int, int, void*);
