@@ -1399,11 +1399,10 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
   T* coefs = rows + 3 * max_n;                  // kMaxKeep
   T* tw = coefs + kMaxKeep;                     // 2 * max_n twiddles
   T* redT = staging + staging_words;            // 64, then 64 doubles
-  __shared__ MemberDev<T> smd;
-
   const WorkItem w = wl[blockIdx.x];
-  load_member(mems, w.member, &smd);
-  const MemberDev<T>& md = smd;
+  // The member descriptor is read in place (read-only, L1-cached): copying
+  // it to shared memory cost a barrier per block.
+  const MemberDev<T>& md = mems[w.member];
   const int N = md.N, M = md.M, Mh = md.Mh;
   const T* gd_in = md.st[a.in_slot][F_GD];
   const T* iu_in = md.st[a.in_slot][F_IU];

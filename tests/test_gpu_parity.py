@@ -221,3 +221,19 @@ def test_weno_batch_mixed_grids_parity_and_fp32(native):
             assert np.array_equal(interior(a), interior(r))
     for a, b in zip(runs[gdc.FP32], runs[gdc.FP64]):
         assert rel_l2(a[2], b[2]) <= 1e-5
+
+
+def test_iap_and_derived_state_read_back_bitwise(native):
+    """gdc_get_iap / gdc_get_state after steps: iap u, iap v, iap gd = sqrt(gd)
+    and the recovered u, v equal the oracle's state arrays bit for bit."""
+    N, M = 180, 91
+    p = scheme(gdc, N, M, 480.0, cutoff=(3, 3, 3))
+    m, o = pair(p, gdc.ic_seeded(N, M, seed=8))
+    m.run(3)
+    o.step(3)
+    s = o.get_state()
+    iu, iv, ig = m.get_iap()
+    u, v, gd = m.get_state()
+    for a, name in ((iu, "iu"), (iv, "iv"), (ig, "ig"), (u, "u"), (v, "v"), (gd, "gd")):
+        assert np.array_equal(interior(a), interior(s[name])), name
+    m.close()
