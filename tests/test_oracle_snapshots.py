@@ -1,0 +1,39 @@
+"""Oracle regression snapshots (CPU): the reference's Rossby-Haurwitz wave
+and mountain zonal flow test cases run one model day at 2 degrees (180 x 91,
+dt 480 s, csp2 with 6 subcycles, cutoffs 4, 4, 4) without NaN, with mass
+and energy conserved to round-off, and end in the committed states (SHA-256
+of the interior u, v, gd bytes).  A change of the oracle's arithmetic shows
+here first; the hashes are those of this container's build (x86-64, no FMA
+contraction)."""
+import hashlib
+import platform
+
+import numpy as np
+import pytest
+
+import gdc
+from helpers import interior
+from oracle.oracle import OracleModel
+
+SNAPSHOTS = {
+    "rossby_haurwitz": "c78b6c1fcf4124f5b919f4314cc7c6b3593652ebf85eef199a00cff4eafa8715",
+    "mountain_zonal_flow": "690c1babf1773359f1b23371e84074ff145f6dec68b8b1766a99f34bf40025f5",
+}
+
+
+@pytest.mark.parametrize("case", sorted(SNAPSHOTS))
+def test_one_day_snapshot(case):
+    N, M = 180, 91
+    ic = gdc.ic_rossby_haurwitz(N, M) if case == "rossby_haurwitz" else gdc.ic_mountain_zonal_flow(N, M)
+    o = OracleModel(N, M, 480.0, subcycles=6, split_scheme=2, cutoff=[4, 4, 4])
+    o.set_state(*ic)
+    m0, e0, _ = o.diag()
+    assert o.step(180) == 0
+    m1, e1, beta = o.diag()
+    assert abs(m1 - m0) <= 1e-12 * m0 and abs(e1 - e0) <= 1e-9 * e0
+    assert 0.99 < beta < 1.01
+    s = o.get_state()
+    digest = hashlib.sha256(b"".join(np.ascontiguousarray(interior(s[k])).tobytes()
+                                     for k in ("u", "v", "gd"))).hexdigest()
+    if platform.machine() in ("x86_64", "AMD64"):
+        assert digest == SNAPSHOTS[case]
