@@ -400,7 +400,7 @@ namespace {
 using gdc::kOmega;
 using gdc::kPi;
 using gdc::kRadius;
-constexpr double kG = 9.80616;  // src/params_mod.F90:11
+constexpr double kG = gdc::kGrav;
 
 // Padded-layout helpers: Fortran (i,j) = (i0+1, j0+1) for 0-based interior.
 inline double& P(double* f, int ld, int i0, int j0) { return f[(size_t)(j0 + 2) * ld + (i0 + 2)]; }
