@@ -229,7 +229,8 @@ def profile_kernels(gdc, members, precision, nsteps=2):
 
 
 def plain_fp64(gdc, torch, ts, steps=360):
-    """Config 0 through the plain FP64 path (one member, 360 steps)."""
+    """The seeded 360x181 state (dt 240 s) through the plain FP64 path: one
+    member, 360 steps."""
     N, M, dt, _, cut = GRIDS[360]
     ic = gdc.ic_seeded(N, M, seed=0)
     p = gdc.default_params(num_lon=N, num_lat=M, time_step_size=dt, subcycles=6, split_scheme=gdc.SPLIT_CSP2,

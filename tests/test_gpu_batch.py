@@ -46,7 +46,7 @@ def test_batch_member_matches_single_model(native, prec):
 
 
 def test_fp32_compensated_vs_fp64(native):
-    """Config 1 (720x361, dt 120 s, mountains + zonal flow), one model day:
+    """Zonal flow over three mountains on 720x361 (dt 120 s), one model day:
     FP32 with compensated time levels vs the FP64 path; gd relative L2
     <= 1e-5 (the stated bound).  The zonal flow makes the reference's
     filter rescale noise-driven on filtered rows, so both runs use the

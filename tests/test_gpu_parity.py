@@ -5,8 +5,8 @@ so every point-wise expression rounds exactly as the oracle's, and every
 sum (filter s1/s2 and projections, pole caps, beta, diagnostics) is the
 correctly rounded sum on both sides.  The plain path is therefore expected
 to be bitwise identical to the oracle; the stated bound (relative L2
-<= 1e-12 after 360 steps of config 0, mass drift equal within 1e-13) is
-asserted as well.
+<= 1e-12 after 360 steps of the seeded 360x181 state, mass drift equal
+within 1e-13) is asserted as well.
 """
 import numpy as np
 import pytest
@@ -80,8 +80,8 @@ def test_diffusion_parity(native):
 
 
 @pytest.mark.slow
-def test_config0_360_steps(native):
-    """Config 0: 360x181, dt=240 s, 360 steps, filter on, no topography."""
+def test_seeded_360x181_one_day(native):
+    """The seeded state on 360x181, dt=240 s, 360 steps, filter on, no topography."""
     N, M = 360, 181
     p = scheme(gdc, N, M, 240.0)
     ic = gdc.ic_seeded(N, M, seed=0)
