@@ -274,6 +274,66 @@ def stage_traffic():
         return None
 
 
+def beside_path(gdc, torch):
+    """Timings of the rows beside the hot path (host-visible, CUDA-synchronised
+    wall clock): admitting a 1440x721 FP32 member from host arrays vs
+    generating its state on the device; checkpoint, restore and the history
+    fields of that member; and the WENO advection option against the centred
+    scheme on 64 x 180x91 FP32 members (no splitting, dt 90 s, 8 steps after
+    2 warm-up steps: the range in which the reference's WENO stays stable)."""
+    out = {}
+
+    def timed(f):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = f()
+        torch.cuda.synchronize()
+        return r, (time.perf_counter() - t0) * 1e3
+
+    try:
+        N, M, dt, _, cut = GRIDS[1440]
+        b = gdc.Batch(scheme(gdc, gdc.FP32, subcycles=8))
+        spec = gdc.ic_spec(gdc.IC_SEEDED, seed=1, noise_seed=7, noise_sigma=gdc.G)
+
+        def host_add():
+            ic = gdc.ic_seeded(N, M, seed=1)
+            gdc.ic_add_noise(ic[2], N, M, 7, gdc.G)
+            return b.add(N, M, dt, 4, *ic, cutoff=cut)
+
+        _, host_ms = timed(host_add)
+        idv, dev_ms = timed(lambda: b.add_ic(N, M, dt, 4, spec, cutoff=cut))
+        with tempfile.TemporaryDirectory() as d:
+            path = os.path.join(d, "member.rst")
+            _, ck_ms = timed(lambda: b.checkpoint(idv, path))
+            _, rs_ms = timed(lambda: b.restore(path))
+        _, hist_ms = timed(lambda: b.history(idv))
+        b.close()
+        out["admission_1440x721_ms"] = {"host_arrays": host_ms, "device_generated": dev_ms}
+        out["checkpoint_1440x721_ms"] = ck_ms
+        out["restore_1440x721_ms"] = rs_ms
+        out["history_fields_1440x721_ms"] = hist_ms
+        rates, nans = {}, {}
+        ic = gdc.ic_seeded(180, 91, seed=2)
+        for name, adv in (("center_diff", gdc.ADV_CENTER_DIFF), ("weno", gdc.ADV_WENO)):
+            q = gdc.default_params(num_lon=180, num_lat=91, time_step_size=90.0, subcycles=6,
+                                   split_scheme=gdc.SPLIT_NONE, qcon_modified=1, uv_adv_scheme=adv,
+                                   use_zonal_tend_filter=1, zonal_tend_filter_cutoff_wavenumber=[3] * 3,
+                                   precision=gdc.FP32)
+            bb = gdc.Batch(q)
+            ids = [bb.add(180, 91, 90.0, 10, *ic) for _ in range(64)]
+            bb.step(2)
+            bb.sync()
+            _, ms = timed(lambda: (bb.step(8), bb.sync()))
+            rates[name] = 64 * 180 * 91 * 8 / (ms / 1e3)
+            nans[name] = sum(1 for i in ids if bb.info(i)[2] >= 0)
+            bb.close()
+        out["uv_adv_scheme_grid_pt_steps_per_s"] = rates
+        out["uv_adv_scheme_nan_members"] = nans
+    except Exception as e:  # a failure here must not cost the headline line
+        out["error"] = repr(e)
+    return out
+
+
 def serve_sample(gdc, ts, n=40, rate=20.0, seed=0):
     """The serving loop on the first `n` requests of the Poisson stream
     (20 requests/s; grids 180x91..1440x721; 6 h to 5 days), FP32."""
@@ -384,6 +444,7 @@ def run_ours(args, rank, world, dist):
     serving = serve_sample(gdc, ts) if rank == 0 else None
     if rank != 0:
         return
+    beside = beside_path(gdc, torch)
     # Roofline of the dominant kernel (the fused stage kernel): algorithmic
     # bytes per launch = 10 prognostic words per grid point (stages read+write
     # 7, 13 and 10 words: 30 over 3 launches) x 4 bytes x active points.
@@ -430,6 +491,7 @@ def run_ours(args, rank, world, dist):
                        "l2_fp32_vs_fp64_after_1_day": plain["l2_fp32_vs_fp64"],
                        "batched_fp32_over_plain_fp64": value / plain["value"]},
         "serving": serving,
+        "beside_path": beside,
         "nan_members": sum(1 for x in nan if x >= 0),
         "cpu_baseline": cpu_baseline_sample(),
     }
