@@ -313,3 +313,26 @@ def test_diffusion_known_answers():
     s = o.get_state()
     assert np.all(interior(s["u"]) == 0) and np.all(interior(s["v"]) == 0)
     assert np.array_equal(interior(s["gd"]), interior(gd))
+
+
+def test_upwind_with_zero_beta_is_centred():
+    """The upwind advection (src/dycore_mod.F90:393-415, :450-469) with
+    uv_adv_upwind_lon/lat_beta = 0 is the centred scheme rewritten:
+    u2 (ic + ip) - u1 (ic + im) - (u2 - u1) ic = u2 ip - u1 im.  Equal to
+    round-off; with beta > 0 it differs (the upwind dissipation)."""
+    N, M = 72, 37
+    ic = _seeded(N, M, seed=12)
+
+    def slow(adv, beta):
+        o = OracleModel(N, M, 600.0, split_scheme=2, uv_adv_scheme=adv, upwind_lon_beta=beta, upwind_lat_beta=beta,
+                        use_zonal_tend_filter=0, cutoff=[])
+        o.set_state(*ic)
+        du, dv, _ = o.tendency(2)
+        return interior(du), interior(dv)
+
+    cu, cv = slow(0, 0.0)
+    uu, uv = slow(1, 0.0)
+    assert np.max(np.abs(uu - cu)) <= 1e-12 * np.max(np.abs(cu))
+    assert np.max(np.abs(uv - cv)) <= 1e-12 * np.max(np.abs(cv))
+    bu, _ = slow(1, 0.5)
+    assert np.max(np.abs(bu - cu)) > 1e-3 * np.max(np.abs(cu))
