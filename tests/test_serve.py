@@ -46,6 +46,7 @@ class FakeBatch:
         self.members = {}
         self.next_id = 0
         self.adds = []
+        self.specs = []
 
     def add(self, N, M, dt, nsteps, u, v, gd, ghs, reserve_bytes=0, cutoff=None):
         if len(self.members) >= self.capacity:
@@ -55,6 +56,10 @@ class FakeBatch:
         self.members[mid] = [0, nsteps]
         self.adds.append((mid, N, nsteps))
         return mid
+
+    def add_ic(self, N, M, dt, nsteps, spec, reserve_bytes=0, cutoff=None):
+        self.specs.append(spec)
+        return self.add(N, M, dt, nsteps, None, None, None, None, reserve_bytes, cutoff)
 
     def step(self, n):
         for _ in range(n):
@@ -123,3 +128,18 @@ def test_server_raises_when_a_request_can_never_fit():
     srv, fb, clock = fake_server(capacity=0)
     with pytest.raises(gdc.GdcError):
         srv.run([serve.Request(rid=0, grid=180, nsteps=1, arrival=0.0)])
+
+
+def test_device_initial_states_go_through_add_ic():
+    """The default initial states are specs of the seeded state generated on
+    the device (one noise seed per request); the server admits them with
+    add_ic, and host-built states with add."""
+    reqs = [serve.Request(rid=k, grid=360, nsteps=2, arrival=0.0) for k in range(3)]
+    clock = FakeClock()
+    fb = FakeBatch(clock, capacity=5)
+    srv = serve.Server(steps_per_tick=2, batch_factory=lambda: fb, clock=clock, sleep=clock.sleep)
+    stats = srv.run(reqs)
+    assert stats["completed"] == 3
+    assert [sp.kind for sp in fb.specs] == [gdc.IC_SEEDED] * 3
+    assert [sp.noise_seed for sp in fb.specs] == [1000, 1001, 1002]
+    assert all(sp.noise_sigma == pytest.approx(gdc.G) for sp in fb.specs)
