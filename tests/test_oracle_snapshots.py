@@ -1,7 +1,8 @@
 """Oracle regression snapshots (CPU): the reference's Rossby-Haurwitz wave
 and mountain zonal flow test cases run one model day at 2 degrees (180 x 91,
 dt 480 s, csp2 with 6 subcycles, cutoffs 4, 4, 4) without NaN, with mass
-and energy conserved to round-off, and end in the committed states (SHA-256
+and energy conserved to round-off, the RH pattern moving east at its
+analytic rate, and end in the committed states (SHA-256
 of the interior u, v, gd bytes).  A change of the oracle's arithmetic shows
 here first; the hashes are those of this container's build (x86-64, no FMA
 contraction)."""
@@ -37,3 +38,15 @@ def test_one_day_snapshot(case):
                                      for k in ("u", "v", "gd"))).hexdigest()
     if platform.machine() in ("x86_64", "AMD64"):
         assert digest == SNAPSHOTS[case]
+    if case == "rossby_haurwitz":
+        # The wave-4 pattern travels east at about the non-divergent rate
+        # nu = (R (3 + R) omega - 2 Omega) / ((1 + R)(2 + R)) (Haurwitz 1940;
+        # the shallow-water wave runs a little slower): within 15 % after a
+        # day, with its amplitude kept to 5 %.
+        R, w, Om = 4.0, 7.848e-6, 2 * np.pi / 86400
+        want = R * (R * (3 + R) * w - 2 * Om) / ((1 + R) * (2 + R)) * 86400
+        f0 = np.fft.rfft(interior(ic[2]), axis=1)[:, 4]
+        f1 = np.fft.rfft(interior(s["gd"]), axis=1)[:, 4]
+        shift = -np.angle(np.sum(f1 * np.conj(f0)))
+        assert abs(shift - want) < 0.15 * want
+        assert abs(np.linalg.norm(f1) / np.linalg.norm(f0) - 1) < 0.05
