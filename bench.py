@@ -13,7 +13,7 @@ steps per second over the timed steps with the inputs resident in HBM; the
 plain FP64 path (360x181, 360 steps) is timed beside it.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload batch|plain|serve]
+                  [--workload batch|plain|large-run]
 
 --impl reference times the CPU oracle (the restatement of the reference's
 Fortran, which cannot be built here) on the host cores over a bounded
@@ -392,6 +392,39 @@ def large_run(args):
     print(json.dumps(out), flush=True)
 
 
+def plain_run(args):
+    """The plain FP64 path alone: the seeded 360x181 state, dt 240 s, csp2
+    with 6 subcycles, for --steps steps (default one model day) after
+    --warmup steps, timed with CUDA events.  Short runs of this workload
+    are the FP64 profiling case."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    import gdc
+    ts = torch.cuda.Stream()
+    N, M, dt, spd, cut = GRIDS[360]
+    steps = args.steps if args.steps_given else spd
+    ic = gdc.ic_seeded(N, M, seed=0)
+    p = gdc.default_params(num_lon=N, num_lat=M, time_step_size=dt, subcycles=6, split_scheme=gdc.SPLIT_CSP2,
+                           qcon_modified=1, zonal_tend_filter_cutoff_wavenumber=cut, precision=gdc.FP64)
+    m = gdc.Model(p)
+    m.set_stream(ts.cuda_stream)
+    m.set_state(*ic)
+    m.run(args.warmup)
+    m.set_state(*ic)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(ts)
+    m.step(steps)
+    e1.record(ts)
+    torch.cuda.synchronize()
+    m.sync()
+    ms = e0.elapsed_time(e1)
+    m.close()
+    print(json.dumps({"workload": "plain", "grid": f"{N}x{M}", "dtype": "f64", "steps": steps,
+                      "value": N * M * steps / (ms / 1e3), "unit": "grid-pt-steps/s", "ms": ms}), flush=True)
+
+
 def cpu_baseline_sample(seconds_target=12.0):
     """The oracle (port of the reference, 1 thread) on a 360x181 member."""
     import gdc
@@ -565,14 +598,16 @@ def main():
     ap.add_argument("--steps", type=int, default=720)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="batch", choices=["batch", "large-run"],
-                    help="large-run: 1440x721 FP32 for --days model days with per-day mass and energy drift, "
+    ap.add_argument("--workload", default="batch", choices=["batch", "plain", "large-run"],
+                    help="plain: the FP64 path alone on the seeded 360x181 state; "
+                         "large-run: 1440x721 FP32 for --days model days with per-day mass and energy drift, "
                          "beside the FP64 path for --fp64-days")
     ap.add_argument("--days", type=int, default=10)
     ap.add_argument("--fp64-days", type=int, default=2)
     ap.add_argument("--profile-only", action="store_true",
                     help="run warmup+steps of the ensemble batch and exit (for ncu)")
     args = ap.parse_args()
+    args.steps_given = any(a == "--steps" or a.startswith("--steps=") for a in sys.argv[1:])
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     rank, world, dist = dist_setup(args.gpus) if args.impl == "ours" else (
@@ -581,6 +616,8 @@ def main():
         run_reference(args, rank, world, dist)
     elif args.workload == "large-run":
         large_run(args)
+    elif args.workload == "plain":
+        plain_run(args)
     else:
         run_ours(args, rank, world, dist)
     if dist is not None:

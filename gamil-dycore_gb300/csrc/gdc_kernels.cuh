@@ -30,6 +30,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 
@@ -2082,6 +2083,31 @@ __global__ void __launch_bounds__(kThreads)
 
 // --------------------------------------------------------- launchers
 
+// Dynamic shared memory already allowed for one kernel, per device: the
+// attribute is a per-device setting, and launches may come from several
+// host threads (one batch engine each).
+struct SmemConfigured {
+  static constexpr int kDevices = 64;
+  std::atomic<size_t> bytes[kDevices];
+  SmemConfigured() {
+    for (auto& b : bytes) b.store(0);
+  }
+  // True when `smem` bytes are already allowed on the current device.
+  bool covers(size_t smem, int* dev) {
+    if (cudaGetDevice(dev) != cudaSuccess || *dev < 0 || *dev >= kDevices) {
+      *dev = -1;
+      return false;
+    }
+    return smem <= bytes[*dev].load();
+  }
+  void record(int dev, size_t smem) {
+    if (dev < 0) return;
+    size_t cur = bytes[dev].load();
+    while (smem > cur && !bytes[dev].compare_exchange_weak(cur, smem)) {
+    }
+  }
+};
+
 static inline int check_launch() {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
@@ -2115,12 +2141,13 @@ static int launch_stage_t(const MemberDev<T>* mem, const WorkItem* wl, int nwork
   int sw = 0;
   max_n = (max_n + 1) & ~1;
   const size_t smem = stage_smem_bytes<T>(R, W, max_n, &sw);
-  static size_t configured = 0;
-  if (smem > configured) {
+  static SmemConfigured configured;
+  int dev = -1;
+  if (!configured.covers(smem, &dev)) {
     if (cudaFuncSetAttribute(stage_kernel<T, PASS, ADV, R, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem) != cudaSuccess)
       return check_launch();
-    configured = smem;
+    configured.record(dev, smem);
   }
   stage_kernel<T, PASS, ADV, R, W><<<nwork, kThreads, smem, s>>>(mem, wl, a, sw, max_n);
   return check_launch();
@@ -2333,7 +2360,8 @@ int launch_diffusion(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int
   int sw = 0;
   max_n = (max_n + 1) & ~1;
   const size_t smem = stage_smem_bytes<T>(tile_rows, tile_cols, max_n, &sw);
-  static size_t configured = 0;
+  static SmemConfigured configured;
+  int dev = -1;
   auto lap = diffusion_lap_kernel<T, 8, 32>;
   if (tile_rows == 8 && tile_cols == 64)
     lap = diffusion_lap_kernel<T, 8, 64>;
@@ -2341,11 +2369,11 @@ int launch_diffusion(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int
     lap = diffusion_lap_kernel<T, 4, 128>;
   else if (!(tile_rows == 8 && tile_cols == 32))
     return GDC_E_CONFIG;
-  if (smem > configured) {
+  if (!configured.covers(smem, &dev)) {
     for (auto k : {diffusion_lap_kernel<T, 8, 32>, diffusion_lap_kernel<T, 8, 64>, diffusion_lap_kernel<T, 4, 128>})
       if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return check_launch();
-    configured = smem;
+    configured.record(dev, smem);
   }
   lap<<<nwork, kThreads, smem, s>>>(mem, wl, slot, sign_dt_coef, sw, max_n);
   int rc = check_launch();

@@ -1,17 +1,16 @@
 // gdc_noalloc.cu -- the space_operators tendency for callers that cannot
 // allocate device memory.
 //
-// Some callers of this library cannot call cudaMalloc: code running while a
-// stream is being captured into a CUDA graph (an allocation there breaks
-// the capture), host frameworks that own every device allocation through
-// their own pool and forbid others, and plug-ins that must not grow the
-// process's device footprint once running.  gdc_tendency_noalloc serves
-// them: the caller passes its own device buffers for the state and for the
-// tendencies, and everything else the stage kernel needs (member
-// descriptor, work list, row coefficient tables, filter twiddles, the
-// given-u/v marker) lives in one file-scope device array of fixed size,
-// loaded with the library and held by every GPU that loads it until the
-// process exits.
+// Some callers of this library cannot call cudaMalloc: host frameworks that
+// own every device allocation through their own pool and forbid others,
+// processes that run under a fixed device-memory budget, and plug-ins that
+// must not grow the process's device footprint once running.
+// gdc_tendency_noalloc serves them: the caller passes its own device
+// buffers for the state and for the tendencies, and everything else the
+// stage kernel needs (member descriptor, work list, row coefficient
+// tables, filter twiddles, the given-u/v marker) lives in one file-scope
+// device array of fixed size, loaded with the library and held by every
+// GPU that loads it until the process exits.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -33,9 +32,12 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratch
 namespace {
 
 constexpr int kMaxDevices = 64;
+// Guards the per-device addresses and serialises the calls' uploads into
+// the shared array.
 std::mutex g_mu;
 void* g_scratch_addr[kMaxDevices] = {nullptr};
-std::string g_err;
+// The calling thread's last failure (read without the lock).
+thread_local std::string g_err;
 
 size_t up256(size_t x) { return (x + 255) & ~size_t(255); }
 

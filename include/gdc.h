@@ -2,9 +2,9 @@
  * gdc.h -- C ABI of the GB300-native gamil-dycore barotropic time step.
  *
  * Plain C types only (ints, doubles, pointers, sizes): the reference's
- * Fortran host binds it through ISO_C_BINDING, Python
- * through ctypes.  Every call returns GDC_OK (0) or a GDC_E_* code and never
- * exits the process; the message of the last failure is available from
+ * Fortran host binds it through ISO_C_BINDING, Python through ctypes.
+ * Every call returns GDC_OK (0) or a GDC_E_* code and never exits the
+ * process; the message of the last failure is available from
  * gdc_last_error / gdc_batch_last_error.
  *
  * Host field layout ("padded layout"): the reference's own allocation,
@@ -158,10 +158,11 @@ int gdc_debug_tendency(gdc_handle* h, int pass, double* du, double* dv,
 int gdc_set_stream(gdc_handle* h, void* cuda_stream);
 
 /* No counterpart in the reference: space_operators (as gdc_debug_tendency)
- * for callers that cannot allocate device memory -- code inside CUDA-graph
- * stream capture, hosts whose allocator owns all device memory, plug-ins
- * that must not grow the device footprint.  FP64 only.  All pointers are
- * the CALLER's device buffers in the interior layout (rows x num_lon,
+ * for callers that cannot allocate device memory -- hosts whose allocator
+ * owns every device allocation (a framework's caching pool, a memory
+ * budget enforced per process), and plug-ins that must not grow the
+ * device footprint once running.  FP64 only.  All pointers are the
+ * CALLER's device buffers in the interior layout (rows x num_lon,
  * longitude fastest, no halo): gd, iap_u, ghs, du, dgd num_lat rows;
  * iap_v, dv num_lat-1 rows; given_u/given_v (both or neither) are u, v to
  * use as given (e.g. an initial condition's own u, v), NULL to derive them
@@ -169,11 +170,13 @@ int gdc_set_stream(gdc_handle* h, void* cuda_stream);
  * tables in one 2 MiB static device array (held by every GPU that loads the
  * library until exit), so grids are limited to 1440 x 721; larger grids
  * return GDC_E_CONFIG.  It calls no cudaMalloc / cudaFree.  The first call
- * on a device resolves the array's device address -- make it before any
- * stream capture.  All calls share the array: calls that overlap on the
- * GPU race (serialise them on one stream).  Enqueued on `cuda_stream`;
- * returns before the kernel finishes.  The message of a failure is
- * gdc_noalloc_last_error(). */
+ * on a device resolves the array's device address (set-up); make that
+ * first call before any stream capture.  Each call uploads its tables from
+ * host memory with cudaMemcpyAsync on `cuda_stream`.  All calls share the
+ * array and each rewrites it: calls that overlap on the GPU race
+ * (serialise them on one stream).  Enqueued on `cuda_stream`; returns
+ * before the kernel finishes.  The message of the calling thread's last
+ * failure is gdc_noalloc_last_error(). */
 int gdc_tendency_noalloc(const gdc_params* p, int pass, const double* gd,
                          const double* iap_u, const double* iap_v,
                          const double* ghs, const double* given_u,

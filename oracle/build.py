@@ -1,11 +1,21 @@
 """Build recipe for the parity oracle (test infrastructure only).
 
-Compiles gdc_oracle.c with gcc into oracle/_build/libgdc_oracle.so at -O2
+Compiles gdc_oracle.c and gdc_fftpack.c with gcc into oracle/_build/ at -O2
 with FMA contraction and fast-math disabled, so that the C evaluation order
-is the order written in the source (which follows the reference's).  The
-reference (Fortran 2003) itself cannot be compiled here: no Fortran compiler
-exists on either machine, and its datetime/container submodules and NetCDF
-are absent.
+is the order written in the source (which follows the reference's):
+
+* libgdc_oracle.so -- the checker: correctly rounded sums, the filter as a
+  projection onto the kept modes (the CUDA path's arithmetic);
+* libgdc_oracle_ref.so -- the reference's order: plain running sums in the
+  reference's loop order (-DGDO_PLAIN_SUMS); with gdo_set_fft the filter
+  runs FFTPACK's transforms as the reference does;
+* libgdc_oracle_fast.so -- the same reference-order arithmetic compiled
+  with the reference's own flags (-Ofast, CMakeLists.txt:13): the timed CPU
+  baseline, never a checker.
+
+The reference (Fortran 2003) itself cannot be compiled here: no Fortran
+compiler exists on either machine, and its datetime/container submodules
+and NetCDF are absent.
 """
 from __future__ import annotations
 
@@ -14,25 +24,28 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_build"
-SRC = HERE / "gdc_oracle.c"
+SRCS = [HERE / "gdc_oracle.c", HERE / "gdc_fftpack.c"]
+HDRS = [HERE / "gdc_oracle.h", HERE / "gdc_fftpack.h"]
 LIB = OUT / "libgdc_oracle.so"
-# Timing variant for the CPU baseline: plain running sums, compiled with the
-# reference's own optimisation flags (-Ofast, CMakeLists.txt:13).  Never
-# used as a checker.
+LIB_REF = OUT / "libgdc_oracle_ref.so"
 LIB_FAST = OUT / "libgdc_oracle_fast.so"
+EXACT = ["-O2", "-ffp-contract=off", "-fno-fast-math"]
+LIBS = {"exact": (LIB, EXACT),
+        "ref": (LIB_REF, EXACT + ["-DGDO_PLAIN_SUMS"]),
+        "fast": (LIB_FAST, ["-Ofast", "-DGDO_PLAIN_SUMS"])}
 
 
 def _compile(out: Path, flags: list[str], force: bool) -> None:
-    newest = max(SRC.stat().st_mtime, (HERE / "gdc_oracle.h").stat().st_mtime)
+    newest = max(p.stat().st_mtime for p in SRCS + HDRS)
     if force or not out.exists() or out.stat().st_mtime < newest:
-        cmd = ["gcc", *flags, "-std=c99", "-fPIC", "-shared", "-o", str(out), str(SRC), "-lm"]
+        cmd = ["gcc", *flags, "-std=c99", "-fPIC", "-shared", "-o", str(out), *map(str, SRCS), "-lm"]
         subprocess.run(cmd, check=True)
 
 
 def build(force: bool = False) -> Path:
     OUT.mkdir(exist_ok=True)
-    _compile(LIB, ["-O2", "-ffp-contract=off", "-fno-fast-math"], force)
-    _compile(LIB_FAST, ["-Ofast", "-DGDO_PLAIN_SUMS"], force)
+    for out, flags in LIBS.values():
+        _compile(out, flags, force)
     return LIB
 
 

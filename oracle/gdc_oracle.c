@@ -20,10 +20,19 @@
  * fixed -- it is built with -Ofast, which lets the compiler reassociate --
  * and the correctly rounded sum is the order-independent value every
  * order approximates; the CUDA path computes the same value.
+ *
+ * Reference-order build (-DGDO_PLAIN_SUMS, compiled -O2 without
+ * contraction): every reduction is instead the reference's own running sum
+ * in its loop order (s = s + term, j outer, i inner), and with
+ * gdo_set_fft(m, 1) the filter runs FFTPACK's transforms (gdc_fftpack.c)
+ * instead of the projection -- the reference's arithmetic as written,
+ * evaluated in source order.
  */
 #include "gdc_oracle.h"
 
 #include <math.h>
+
+#include "gdc_fftpack.h"
 #include <stdlib.h>
 #include <string.h>
 
@@ -62,6 +71,12 @@ struct gdo_model {
   int use_diff, diff_order;
   double diff_coef;
   double rescale_rtol; /* extension guard, 0 = reference behaviour */
+  /* Conditioning record of the s1/s2 rescale (diagnostic): the largest
+   * sum|t w| / |s| seen for s1 and s2 since the last gdo_rescale_record
+   * call, and where (field: 0 du, 1 dv, 2 dgd; Fortran row index). */
+  double rc_cond[2];
+  int rc_field[2], rc_row[2];
+  int cur_field, cur_row;
   /* mesh (1-based; index 0 and R+1 are zero pads standing for the
    * out-of-bounds reads described at v_adv_lat) */
   double dlon, dlat;
@@ -77,6 +92,12 @@ struct gdo_model {
   int *flag_full, *flag_half;    /* 1-based */
   double *ffac_full, *ffac_half; /* [lat][N], 1-based lat, 0-based lon */
   double *ctab, *stab;           /* cos/sin(2 pi m / N), m = 0..N-1 */
+  /* Filter arithmetic: 0 = projection onto the kept modes (the CUDA
+   * path's), 1 = FFTPACK's forward and backward transforms (the
+   * reference's, gdc_fftpack.c). */
+  int fft;
+  gdo_rfft plan;
+  double *fft_r, *fft_w;
   /* WENO scratch, src/weno_mod.F90:26-31: split and interface fluxes
    * (u-shaped fp_u, fn_u, f_u; v-shaped fp_v, fn_v, f_v).  Zeroed once
    * (parallel_allocate, src/parallel_mod.F90:312-313); the pole and
@@ -329,6 +350,45 @@ gdo_model* gdo_create(int num_lon, int num_lat, double time_step_size,
 
 void gdo_set_rescale_rtol(gdo_model* m, double rtol) { m->rescale_rtol = rtol; }
 
+void gdo_rescale_record(gdo_model* m, double* cond, int* field, int* row) {
+  for (int k = 0; k < 2; ++k) {
+    cond[k] = m->rc_cond[k];
+    field[k] = m->rc_field[k];
+    row[k] = m->rc_row[k];
+    m->rc_cond[k] = 0.0;
+  }
+}
+
+int gdo_set_fft(gdo_model* m, int on) {
+  if (!on) {
+    m->fft = 0;
+    return 0;
+  }
+  if (!m->plan.ok) {
+    if (gdo_rfft_init(&m->plan, m->N) != 0) return -1;
+    m->fft_r = zalloc(m->N);
+    m->fft_w = zalloc(m->N);
+  }
+  m->fft = 1;
+  return 0;
+}
+
+int gdo_rfft_row(int n, int backward, double* x) {
+  gdo_rfft p;
+  if (gdo_rfft_init(&p, n) != 0) {
+    gdo_rfft_free(&p);
+    return -1;
+  }
+  double* w = zalloc(n);
+  if (backward)
+    gdo_rfft_backward(&p, x, w);
+  else
+    gdo_rfft_forward(&p, x, w);
+  free(w);
+  gdo_rfft_free(&p);
+  return 0;
+}
+
 double gdo_fsum(const double* x, int n) {
   xsum acc;
   xs_init(&acc);
@@ -352,6 +412,8 @@ void gdo_destroy(gdo_model* m) {
   for (int k = 0; k < 5; ++k)
     for (int f = 0; f < T_NFIELD; ++f) free(m->tend_mem[k].a[f]);
   free(m->flag_full); free(m->flag_half);
+  gdo_rfft_free(&m->plan);
+  free(m->fft_r); free(m->fft_w);
   free(m);
 }
 
@@ -364,8 +426,24 @@ void gdo_destroy(gdo_model* m) {
  * r(N) = (1/N) sum x (-1)^n for even N; backward rebuilds x_n = a0 +
  * sum_k (a_k cos + b_k sin) + r(N)(-1)^n.  Coefficients whose factor is 0
  * drop out, so only the kept ones are evaluated. */
+/* src/filter_mod.F90:105-135 as the reference computes it: the row through
+ * rfft1f, times the factor row, back through rfft1b. */
+static void filter_row_fftpack(const gdo_model* m, const double* fac, double* x) {
+  int N = m->N;
+  double *r = m->fft_r, *w = m->fft_w;
+  for (int i = 1; i <= N; ++i) r[i - 1] = x[i + 1];
+  gdo_rfft_forward(&m->plan, r, w);
+  for (int p = 0; p < N; ++p) r[p] = r[p] * fac[p];
+  gdo_rfft_backward(&m->plan, r, w);
+  for (int i = 1; i <= N; ++i) x[i + 1] = r[i - 1];
+}
+
 static void filter_row(const gdo_model* m, const double* fac, double* x) {
   int N = m->N;
+  if (m->fft) {
+    filter_row_fftpack(m, fac, x);
+    return;
+  }
   double* local = zalloc(N);
   double* coefs = zalloc(N);
   for (int i = 1; i <= N; ++i) local[i - 1] = x[i + 1];
@@ -739,6 +817,11 @@ static void filter_tend_row(gdo_model* m, const double* fac, double* trow,
     a1 = a1 + fabs(t);
   }
   s1 = xs_value(&acc);
+  if (fabs(s1) > 1.0e-16 && a1 / fabs(s1) > m->rc_cond[0]) {
+    m->rc_cond[0] = a1 / fabs(s1);
+    m->rc_field[0] = m->cur_field;
+    m->rc_row[0] = m->cur_row;
+  }
   if (fabs(s1) > 1.0e-16) { /* src/filter_mod.F90:31 */
     filter_row(m, fac, trow);
     xs_init(&acc);
@@ -748,6 +831,11 @@ static void filter_tend_row(gdo_model* m, const double* fac, double* trow,
       a2 = a2 + fabs(t);
     }
     s2 = xs_value(&acc);
+    if (a2 / fabs(s2) > m->rc_cond[1]) {
+      m->rc_cond[1] = a2 / fabs(s2);
+      m->rc_field[1] = m->cur_field;
+      m->rc_row[1] = m->cur_row;
+    }
     if (m->rescale_rtol > 0 && (fabs(s1) <= m->rescale_rtol * a1 || fabs(s2) <= m->rescale_rtol * a2)) return;
     for (int i = 1; i <= N; ++i) trow[i + 1] = trow[i + 1] * s1 / s2;
   }
@@ -776,8 +864,11 @@ static void space_operators(gdo_model* m, const state_t* s, tend_t* t, int pass)
   if (pass == ALL_PASS || pass == FAST_PASS) {
     for (int j = 1; j <= M; ++j) {
       for (int i = 1; i <= N; ++i) AT(m, dgd, i, j) = -AT(m, ml, i, j) - AT(m, mt, i, j);
-      if (m->flag_full[j])
+      if (m->flag_full[j]) {
+        m->cur_field = 2;
+        m->cur_row = j;
         filter_tend_row(m, m->ffac_full + (size_t)j * N, ROW(m, dgd, j), ROW(m, s->gd, j), ROW(m, m->ghs, j));
+      }
     }
   } else {
     memset(dgd, 0, full_sz(m) * sizeof(double)); /* :297 */
@@ -791,8 +882,11 @@ static void space_operators(gdo_model* m, const state_t* s, tend_t* t, int pass)
       else
         AT(m, du, i, j) = AT(m, fv, i, j) - AT(m, up, i, j);
     }
-    if (m->flag_full[j])
+    if (m->flag_full[j]) {
+      m->cur_field = 0;
+      m->cur_row = j;
       filter_tend_row(m, m->ffac_full + (size_t)j * N, ROW(m, du, j), ROW(m, s->iu, j), NULL);
+    }
   }
   for (int j = 1; j <= Mh; ++j) {
     for (int i = 1; i <= N; ++i) {
@@ -803,8 +897,11 @@ static void space_operators(gdo_model* m, const state_t* s, tend_t* t, int pass)
       else
         AT(m, dv, i, j) = -AT(m, fu, i, j) - AT(m, vp, i, j);
     }
-    if (m->flag_half[j])
+    if (m->flag_half[j]) {
+      m->cur_field = 1;
+      m->cur_row = j;
       filter_tend_row(m, m->ffac_half + (size_t)j * N, ROW(m, dv, j), ROW(m, s->iv, j), NULL);
+    }
   }
 }
 
@@ -1028,8 +1125,13 @@ static void ordinary_diffusion(gdo_model* m, double dt, state_t* s) {
       xsum acc;
       xs_init(&acc);
       for (int i = 1; i <= N; ++i) {
+#ifdef GDO_PLAIN_SUMS
+        /* np = np - (gd(i,j) - gd(i,j-1)), src/diffusion_mod.F90:126-128 */
+        xs_add(&acc, -(AT(m, gd, i, j) - AT(m, gd, i, j - 1)));
+#else
         xs_add(&acc, -AT(m, gd, i, j));
         xs_add(&acc, AT(m, gd, i, j - 1));
+#endif
       }
       double np = xs_value(&acc);
       double val = np * hc[j - 1] / (m->full_dlat[j] * m->full_dlat[j]) * fc[j] / N;

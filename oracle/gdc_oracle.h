@@ -39,6 +39,18 @@ void gdo_destroy(gdo_model* m);
 /* Extension guard of the filter rescale (0 = reference behaviour); the
  * CUDA path's gdc_params::filter_rescale_rtol. */
 void gdo_set_rescale_rtol(gdo_model* m, double rtol);
+/* Filter arithmetic: on = 0 projects onto the kept modes (default, the
+ * CUDA path's), on = 1 runs FFTPACK 5.1's forward and backward transforms
+ * as the reference does (src/filter_mod.F90:105-167).  Returns -1 when
+ * num_lon has a prime factor above 5. */
+int gdo_set_fft(gdo_model* m, int on);
+/* FFTPACK's rfft1f (backward = 0) or rfft1b (backward = 1) of x[0..n-1] in
+ * place (exposed for its self-test); -1 for an unsupported length. */
+int gdo_rfft_row(int n, int backward, double* x);
+/* Diagnostic: the worst conditioning sum|t w| / |s| of the filter's s1
+ * (index 0) and s2 (index 1) since the last call, with the field (0 du,
+ * 1 dv, 2 dgd) and Fortran row where it occurred; resets the record. */
+void gdo_rescale_record(gdo_model* m, double* cond, int* field, int* row);
 /* The oracle's correctly rounded sum (exposed for its self-test). */
 double gdo_fsum(const double* x, int n);
 

@@ -17,12 +17,19 @@ _libs = {}
 _P = ctypes.POINTER(ctypes.c_double)
 
 
-def lib(fast: bool = False) -> ctypes.CDLL:
-    """The checker (exact sums), or with fast=True the timing build of the
-    CPU baseline (plain sums, -Ofast like the reference)."""
-    if fast not in _libs:
+def lib(kind: str = "exact") -> ctypes.CDLL:
+    """One build of the oracle: "exact" (the checker: correctly rounded sums,
+    the filter as a projection -- the CUDA path's arithmetic), "ref" (the
+    reference's order: plain running sums in its loop order; FFTPACK's
+    transforms with fft=True) or "fast" (the reference-order arithmetic at
+    -Ofast: the timed CPU baseline, never a checker)."""
+    if kind is True:
+        kind = "fast"
+    elif kind is False:
+        kind = "exact"
+    if kind not in _libs:
         _build.build()
-        L = ctypes.CDLL(str(_build.LIB_FAST if fast else _build.LIB))
+        L = ctypes.CDLL(str(_build.LIBS[kind][0]))
         vp, dp, i = ctypes.c_void_p, _P, ctypes.c_int
         ip = ctypes.POINTER(ctypes.c_int)
         L.gdo_create.restype = vp
@@ -30,6 +37,11 @@ def lib(fast: bool = False) -> ctypes.CDLL:
                                  ctypes.c_double, i]
         L.gdo_destroy.argtypes = [vp]
         L.gdo_set_rescale_rtol.argtypes = [vp, ctypes.c_double]
+        L.gdo_set_fft.argtypes = [vp, i]
+        L.gdo_set_fft.restype = i
+        L.gdo_rescale_record.argtypes = [vp, dp, ip, ip]
+        L.gdo_rfft_row.argtypes = [i, i, dp]
+        L.gdo_rfft_row.restype = i
         L.gdo_fsum.argtypes = [dp, i]
         L.gdo_fsum.restype = ctypes.c_double
         L.gdo_set_state.argtypes = [vp, dp, dp, dp, dp]
@@ -43,8 +55,16 @@ def lib(fast: bool = False) -> ctypes.CDLL:
         L.gdo_history.argtypes = [vp, dp, dp, dp, dp, dp]
         L.gdo_filter_row.argtypes = [vp, i, i, dp]
         L.gdo_filter_flags.argtypes = [vp, ip, ip, ip, ip]
-        _lib = L
-    return _lib
+        _libs[kind] = L
+    return _libs[kind]
+
+
+def rfft(x, backward: bool = False) -> np.ndarray:
+    """FFTPACK 5.1's rfft1f (or rfft1b) of one row, as the oracle restates it."""
+    a = np.ascontiguousarray(x, dtype=np.float64).copy()
+    if lib("ref").gdo_rfft_row(len(a), int(backward), _ptr(a)) != 0:
+        raise ValueError(f"length {len(a)} has a prime factor above 5")
+    return a
 
 
 def _ptr(a):
@@ -70,9 +90,14 @@ class OracleModel:
     def __init__(self, num_lon, num_lat, time_step_size, subcycles=4, split_scheme=0, qcon_modified=1,
                  uv_adv_scheme=0, upwind_lon_beta=0.0, upwind_lat_beta=0.5, use_zonal_tend_filter=1,
                  cutoff=(), use_diffusion=0, diffusion_coef=0.0, diffusion_order=2, rescale_rtol=0.0,
-                 fast=False):
+                 fast=False, kind=None, fft=None):
+        """kind: "exact" (default), "ref" or "fast" (see lib()); fft: run the
+        filter through FFTPACK's transforms (default: on for "ref" and
+        "fast", off for "exact")."""
         self.N, self.M = num_lon, num_lat
-        self._L = lib(fast)
+        kind = kind or ("fast" if fast else "exact")
+        self.kind = kind
+        self._L = lib(kind)
         c = (ctypes.c_int * 20)(*([0] * 20))
         for k, x in enumerate(cutoff):
             c[k] = int(x)
@@ -81,14 +106,19 @@ class OracleModel:
                                   use_diffusion, diffusion_coef, diffusion_order)
         if rescale_rtol:
             self._L.gdo_set_rescale_rtol(self.h, rescale_rtol)
+        if fft is None:
+            fft = kind != "exact"
+        if fft and self._L.gdo_set_fft(self.h, 1) != 0:
+            raise ValueError(f"num_lon {num_lon} has a prime factor above 5: no FFTPACK restatement for it")
+        self.fft = bool(fft)
 
     @classmethod
-    def from_params(cls, p):
+    def from_params(cls, p, kind=None, fft=None):
         """Build from a gdc.Params (any object with the same attribute names)."""
         return cls(p.num_lon, p.num_lat, p.time_step_size, p.subcycles, p.split_scheme, p.qcon_modified,
                    p.uv_adv_scheme, p.uv_adv_upwind_lon_beta, p.uv_adv_upwind_lat_beta, p.use_zonal_tend_filter,
                    list(p.zonal_tend_filter_cutoff_wavenumber), p.use_diffusion, p.diffusion_coef,
-                   p.diffusion_order, getattr(p, "filter_rescale_rtol", 0.0))
+                   p.diffusion_order, getattr(p, "filter_rescale_rtol", 0.0), kind=kind, fft=fft)
 
     def set_state(self, u, v, gd, ghs):
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (u, v, gd, ghs)]
@@ -123,6 +153,14 @@ class OracleModel:
         du, dv, dgd = _pad(M, N), _pad(M - 1, N), _pad(M, N)
         self._L.gdo_tendency(self.h, pass_, _ptr(du), _ptr(dv), _ptr(dgd))
         return du, dv, dgd
+
+    def rescale_record(self):
+        """Worst conditioning of the filter rescale since the last call:
+        [(sum|t w| / |s1|, field, row), (same for s2)], field 0 du, 1 dv, 2 dgd."""
+        c = (ctypes.c_double * 2)()
+        f, r = (ctypes.c_int * 2)(), (ctypes.c_int * 2)()
+        self._L.gdo_rescale_record(self.h, c, f, r)
+        return [(c[k], ("du", "dv", "dgd")[f[k]], r[k]) for k in range(2)]
 
     def antisymmetry(self):
         out = np.zeros(4)

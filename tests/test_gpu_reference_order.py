@@ -1,0 +1,114 @@
+"""The plain FP64 path against the reference's own order of arithmetic, and
+on the reference's own namelists.
+
+The CUDA path is bitwise equal to the checker oracle, whose reductions are
+correctly rounded sums and whose polar filter is a projection onto the
+kept modes (test_gpu_parity).  The reference instead adds with running sums
+in its loop order (src/dycore_mod.F90:212-216, 576-591,
+src/types_mod.F90:347-371, src/diag_mod.F90:71-121) and filters with
+FFTPACK 5.1's transforms (src/filter_mod.F90:105-167).  The oracle's
+reference-order build (plain sums, FFTPACK restated in
+oracle/gdc_fftpack.c, -O2 without contraction) evaluates that arithmetic
+in source order, and the CUDA path is compared with it here.
+
+Bounds (FP64): gd relative L2 <= 1e-12 and total-mass drift equal within
+1e-13 after one model day of the seeded 360x181 state.  u and v are held
+to the scheme's own sensitivity: the filter's s1/s2 rescale
+(src/dycore_mod.F90:212-219) is ill-conditioned on some polar rows (s2 is
+1e5-1e6 times smaller than the sum of its terms' magnitudes at some
+steps), so a difference in the last bit anywhere -- the reference's own
+state perturbed by one ulp -- moves u and v by ~1e-11 after a day.  The
+test measures that one-ulp control on the reference-order oracle and
+requires the CUDA path to sit within 10x of it (and below 1e-10).
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import gdc
+from helpers import interior, rel_l2, scheme
+from oracle.oracle import OracleModel
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def one_ulp(gd, seed):
+    """gd with every interior value moved by one ulp, up or down (seeded)."""
+    g = gd.copy()
+    x = g[2:-2, 2:-2]
+    up = np.random.default_rng(seed).random(x.shape) < 0.5
+    g[2:-2, 2:-2] = np.where(up, np.nextafter(x, np.inf), np.nextafter(x, -np.inf))
+    return g
+
+
+def run_ref(p, ic, steps, record=False):
+    o = OracleModel.from_params(p, kind="ref", fft=True)
+    o.set_state(*ic)
+    m0 = o.diag()[0]
+    worst = 0.0
+    for _ in range(steps):
+        assert o.step(1) == 0
+        if record:
+            worst = max(worst, max(c for c, _, _ in o.rescale_record()))
+    s = o.get_state()
+    drift = (o.diag()[0] - m0) / m0
+    o.close()
+    return s, drift, worst
+
+
+@pytest.mark.slow
+def test_seeded_360x181_one_day_against_reference_order(native):
+    N, M, steps = 360, 181, 360
+    p = scheme(gdc, N, M, 240.0)
+    ic = gdc.ic_seeded(N, M, seed=0)
+    m = gdc.Model(p)
+    m.set_state(*ic)
+    g0 = m.diag()[0]
+    m.run(steps)
+    u, v, gd = m.get_state()
+    g_drift = (m.diag()[0] - g0) / g0
+    m.close()
+    ref, r_drift, worst = run_ref(p, ic, steps, record=True)
+    ctl, _, _ = run_ref(p, (ic[0], ic[1], one_ulp(ic[2], 7), ic[3]), steps)
+    err = {"gd": rel_l2(gd, ref["gd"]), "u": rel_l2(u, ref["u"]), "v": rel_l2(v, ref["v"])}
+    control = {f: rel_l2(ctl[f], ref[f]) for f in ("gd", "u", "v")}
+    assert err["gd"] <= 1e-12, (err, control)
+    assert abs(g_drift - r_drift) <= 1e-13, (g_drift, r_drift)
+    for f in ("u", "v"):
+        assert err[f] <= 1e-10 and err[f] <= 10 * control[f], (f, err, control)
+    # the ill-conditioned rescale that sets the control's size
+    assert worst >= 1e4, worst
+
+
+@pytest.mark.parametrize("name,make_ic", [("namelist.mountain", gdc.ic_mountain_zonal_flow),
+                                          ("namelist.rh", gdc.ic_rossby_haurwitz)])
+def test_reference_namelist_one_day(native, name, make_ic):
+    """The reference's mz_test (180x90: no equator row, upwind with lat beta
+    0.1, 8 subcycles, cutoffs 4,4,4) and rh_test (360x180, 10 subcycles,
+    cutoffs 4 x 5) read through the namelist reader and run for one model
+    day from the reference's own initial conditions: bitwise equal to the
+    checker oracle (state, mass, energy, beta), and within rounding of the
+    reference-order oracle."""
+    p, _, _ = gdc.read_namelist(GOLDEN / name)
+    assert p.num_lat % 2 == 0
+    steps = int(round(86400.0 / p.time_step_size))
+    ic = make_ic(p.num_lon, p.num_lat)
+    m = gdc.Model(p)
+    m.set_state(*ic)
+    m.run(steps)
+    u, v, gd = m.get_state()
+    diag = m.diag()
+    m.close()
+    o = OracleModel.from_params(p)
+    o.set_state(*ic)
+    assert o.step(steps) == 0
+    s = o.get_state()
+    for f, a in (("gd", gd), ("u", u), ("v", v)):
+        assert np.array_equal(interior(a), interior(s[f])), (f, rel_l2(a, s[f]))
+    assert diag == o.diag()
+    ref, _, _ = run_ref(p, ic, steps)
+    assert rel_l2(gd, ref["gd"]) <= 1e-12
+    assert rel_l2(u, ref["u"]) <= 1e-10 and rel_l2(v, ref["v"]) <= 1e-10

@@ -1,8 +1,8 @@
 """gdc_tendency_noalloc: the tendency for callers that cannot allocate.
 
-Such callers (code inside CUDA-graph stream capture, hosts whose allocator
-owns all device memory) pass their own device buffers; the library keeps
-its tables in a static device array.  The entry point must give the same
+Such callers (hosts whose allocator owns all device memory, processes under
+a fixed device-memory budget) pass their own device buffers; the library
+keeps its tables in a static device array.  The entry point must give the same
 tendencies as the existing one (gdc_debug_tendency), call after call, and
 must not change the device's free memory once set up.  Collected last so a
 failure here does not stop the other tests.
