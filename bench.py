@@ -15,9 +15,10 @@ plain FP64 path (360x181, 360 steps) is timed beside it.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--workload batch|plain|large-run]
 
---impl reference times the CPU oracle (the restatement of the reference's
-Fortran, which cannot be built here) on the host cores over a bounded
-sample of the same ensemble.
+--impl reference times the reference's arithmetic on the host cores: the
+oracle's reference-order restatement (the Fortran reference cannot be built
+here) advancing the same 64 members for the same --steps and --warmup, one
+process per core, without loading the product library.
 """
 from __future__ import annotations
 
@@ -46,6 +47,10 @@ GRIDS = {
     1440: (1440, 721, 60.0, 1440, [4] * 20),
 }
 ENSEMBLE = [(180, 16), (360, 32), (720, 16)]
+ENSEMBLE_CONFIG = {"workload": "ensemble: 16x180x91@480s + 32x360x181@240s + 16x720x361@120s, one model day each, "
+                               "csp2 m=6, filter on",
+                   "scheme": "predict_correct+csp2(6)+qcon",
+                   "l2_cache": "inputs larger than L2 (working set ~0.8 GB vs 129 MB L2)"}
 
 
 def peaks():
@@ -431,7 +436,7 @@ def cpu_baseline_sample(seconds_target=12.0):
     from oracle.oracle import OracleModel
     N, M, dt, _, cut = GRIDS[360]
     ic = gdc.ic_seeded(N, M, seed=0)
-    o = OracleModel(N, M, dt, subcycles=6, split_scheme=2, qcon_modified=1, cutoff=cut, fast=True)
+    o = OracleModel(N, M, dt, subcycles=6, split_scheme=2, qcon_modified=1, cutoff=cut, kind="fast")
     o.set_state(*ic)
     t0 = time.perf_counter()
     o.step(2)
@@ -441,8 +446,8 @@ def cpu_baseline_sample(seconds_target=12.0):
     o.step(n)
     t = time.perf_counter() - t0
     return {"value": N * M * n / t, "unit": "grid-pt-steps/s", "cores": 1, "kind": "port",
-            "sample": f"oracle port of the reference (FP64, plain sums, -Ofast as the reference's build, "
-                      f"1 thread): one 360x181 member, {n} csp2 steps"}
+            "sample": f"oracle restatement of the reference (FP64, running sums in the reference's order, FFTPACK "
+                      f"transforms, -Ofast as the reference's build, 1 thread): one 360x181 member, {n} csp2 steps"}
 
 
 def run_ours(args, rank, world, dist):
@@ -502,11 +507,8 @@ def run_ours(args, rank, world, dist):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded spherical-harmonic states + per-member N(0,1 m) noise)",
-        "config": {"workload": "ensemble: 16x180x91@480s + 32x360x181@240s + 16x720x361@120s, one model day each, "
-                               "FP32 compensated, csp2 m=6, filter on",
-                   "members": len(members), "grid_pt_steps": gpt, "scheme": "predict_correct+csp2(6)+qcon",
-                   "l2_cache": "inputs larger than L2 (working set ~0.8 GB vs 129 MB L2)",
-                   "parallelism": f"replicas x{world}"},
+        "config": dict(ENSEMBLE_CONFIG, members=len(members), grid_pt_steps=gpt,
+                       parallelism=f"replicas x{world}"),
         "clocks": clocks,
         "e2e": {"value": world * e2e_gpt / (e2e_ms / 1e3), "unit": "grid-pt-steps/s",
                 "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps},
@@ -532,62 +534,141 @@ def run_ours(args, rank, world, dist):
 
 
 # ------------------------------------------------------------- reference
+# The reference's CPU implementation of the path is the oracle's restatement
+# (the Fortran reference cannot be built here): its reference-order build
+# (running sums in the reference's loop order, FFTPACK's transforms in the
+# filter) compiled with the reference's flags (-Ofast).  This process tree
+# never loads the product library: the initial states come from the
+# oracle's own copy of the seeded-state definition (bitwise the library's).
 
-def _ref_member(task):
-    import sys as _s
-    for p in task["paths"]:
-        if p not in _s.path:
-            _s.path.insert(0, p)
-    import gdc
-    from oracle.oracle import OracleModel
-    N, M, dt, nst, cut, seed = task["N"], task["M"], task["dt"], task["nsteps"], task["cutoff"], task["seed"]
-    u, v, gd, ghs = gdc.ic_seeded(N, M, seed=0)
-    gd = gdc.ic_add_noise(gd.copy(), N, M, seed=seed, sigma=1.0 * G)
-    o = OracleModel(N, M, dt, subcycles=6, split_scheme=2, qcon_modified=1, cutoff=cut, fast=True)
-    o.set_state(u, v, gd, ghs)
-    o.step(nst)
-    return N * M * nst
+def _product_library_mapped() -> bool:
+    """Whether this process has the product library (libgdc.so) mapped."""
+    try:
+        with open("/proc/self/maps") as f:
+            return any("libgdc.so" in line for line in f)
+    except OSError:
+        return False
+
+
+def _ref_worker(conn, paths, tasks):
+    """One host process: builds its members' states and oracle models, then
+    advances them by the step counts the parent sends."""
+    for p in paths:
+        if p not in sys.path:
+            sys.path.insert(0, p)
+    from oracle.oracle import OracleModel, ic_add_noise, ic_seeded
+    base, models = {}, []
+    for t in tasks:
+        N, M = t["N"], t["M"]
+        if (N, M) not in base:
+            base[(N, M)] = ic_seeded(N, M, seed=0)
+        u, v, gd, ghs = base[(N, M)]
+        gd = ic_add_noise(gd.copy(), N, M, t["seed"], 1.0 * G)
+        o = OracleModel(N, M, t["dt"], subcycles=6, split_scheme=2, qcon_modified=1, cutoff=t["cutoff"],
+                        kind="fast")
+        o.set_state(u, v, gd, ghs)
+        models.append([o, t["nsteps"], N * M])
+    conn.send(("ready", _product_library_mapped()))
+    while True:
+        n = conn.recv()
+        if n is None:
+            break
+        done, nan = 0, 0
+        for rec in models:
+            k = min(n, rec[1])
+            if k > 0:
+                nan += rec[0].step(k)
+                rec[1] -= k
+                done += rec[2] * k
+        conn.send((done, nan))
+    conn.close()
+
+
+def _plain_reference(seconds_target=10.0):
+    """The plain FP64 configuration (seeded 360x181, dt 240 s, csp2 6) on one
+    host core: the reference-order oracle at -Ofast, bounded sample."""
+    from oracle.oracle import OracleModel, ic_seeded
+    N, M, dt, _, cut = GRIDS[360]
+    o = OracleModel(N, M, dt, subcycles=6, split_scheme=2, qcon_modified=1, cutoff=cut, kind="fast")
+    o.set_state(*ic_seeded(N, M, seed=0))
+    t0 = time.perf_counter()
+    o.step(2)
+    per = (time.perf_counter() - t0) / 2
+    n = max(2, int(seconds_target / per))
+    t0 = time.perf_counter()
+    o.step(n)
+    t = time.perf_counter() - t0
+    return {"value": N * M * n / t, "unit": "grid-pt-steps/s", "cores": 1,
+            "config": "360x181 dt 240 s, FP64, one member", "sample": f"{n} csp2 steps"}
 
 
 def run_reference(args, rank, world, dist):
     if rank != 0:
         return
     import multiprocessing as mp
-    import __graft_entry__
-    __graft_entry__.build()
+    from oracle import build as oracle_build
+    oracle_build.build()
     cores = os.cpu_count() or 1
-    # Bounded sample of the ensemble: every member advances a few steps
-    # (sized so one round is a few seconds on the host cores).
-    per_grid = {180: 8, 360: 4, 720: 2}
     tasks = []
     k = 0
     for g, count in ENSEMBLE:
-        N, M, dt, _, cut = GRIDS[g]
+        N, M, dt, nsteps, cut = GRIDS[g]
         for _ in range(count):
-            tasks.append(dict(N=N, M=M, dt=dt, nsteps=per_grid[g], cutoff=cut, seed=1000 + k,
-                              paths=[str(ROOT), str(ROOT / "gamil-dycore_gb300")]))
+            tasks.append(dict(N=N, M=M, dt=dt, nsteps=args.warmup + nsteps, cutoff=cut, seed=1000 + k))
             k += 1
-    rounds = max(1, min(args.steps, 3))
-    warm = max(0, min(args.warmup, 1))
+    # Members to processes, largest first onto the least loaded (the cost of
+    # a member step is proportional to its grid points).
+    nproc = min(cores, len(tasks))
+    load, parts = [0] * nproc, [[] for _ in range(nproc)]
+    for t in sorted(tasks, key=lambda t: -t["N"] * t["M"]):
+        q = load.index(min(load))
+        parts[q].append(t)
+        load[q] += t["N"] * t["M"]
     ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
-        for _ in range(warm):
-            pool.map(_ref_member, tasks[:cores])
-        t0 = time.perf_counter()
-        done = 0
-        for _ in range(rounds):
-            done += sum(pool.map(_ref_member, tasks))
-        t = time.perf_counter() - t0
+    paths = [str(ROOT)]
+    pipes, procs = [], []
+    for part in parts:
+        a, b = ctx.Pipe()
+        pr = ctx.Process(target=_ref_worker, args=(b, paths, part))
+        pr.start()
+        pipes.append(a)
+        procs.append(pr)
+    mapped = _product_library_mapped()
+    for a in pipes:
+        tag, m = a.recv()
+        assert tag == "ready"
+        mapped = mapped or m
+
+    def advance(n):
+        for a in pipes:
+            a.send(n)
+        got = [a.recv() for a in pipes]
+        return sum(d for d, _ in got), sum(x for _, x in got)
+
+    advance(args.warmup)
+    t0 = time.perf_counter()
+    done, nan = advance(args.steps)
+    t = time.perf_counter() - t0
+    for a in pipes:
+        a.send(None)
+    for pr in procs:
+        pr.join()
     value = done / t
-    sample = (f"oracle port of the reference (FP64, plain sums, -Ofast), {cores} processes over the 64-member ensemble, "
-              f"{rounds} round(s) of 8/4/2 steps per 180x91/360x181/720x361 member")
+    plain = _plain_reference()
+    sample = (f"oracle restatement of the reference (FP64, running sums in the reference's order, FFTPACK "
+              f"transforms, -Ofast as the reference's build), {nproc} processes over the 64-member ensemble, "
+              f"{args.steps} timed steps after {args.warmup} warm-up steps, every member as on the GPU")
     print(json.dumps({
         "impl": "reference",
         "metric": "grid-pt-steps/s batched FP32 vs plain FP64 on GB300 @L2<=1e-5; p50/p99 latency",
         "value": value, "unit": "grid-pt-steps/s", "higher_is_better": True, "n_gpus": world,
-        "steps": rounds, "warmup": warm, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "ensemble: 16x180x91@480s + 32x360x181@240s + 16x720x361@120s (bounded sample)"},
-        "cpu_baseline": {"value": value, "unit": "grid-pt-steps/s", "cores": cores, "kind": "port", "sample": sample},
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3 / max(args.steps, 1),
+        "dtype": "f64", "data": "synthetic (seeded spherical-harmonic states + per-member N(0,1 m) noise)",
+        "config": ENSEMBLE_CONFIG, "grid_pt_steps": done, "nan_members": nan,
+        "product_library_loaded": mapped,
+        "cpu_baseline": {"value": value, "unit": "grid-pt-steps/s", "cores": nproc, "kind": "port",
+                         "sample": sample},
+        "plain_fp64": plain,
         "e2e": {"value": value, "unit": "grid-pt-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
 

@@ -24,7 +24,7 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_build"
-SRCS = [HERE / "gdc_oracle.c", HERE / "gdc_fftpack.c"]
+SRCS = [HERE / "gdc_oracle.c", HERE / "gdc_fftpack.c", HERE / "gdc_oracle_ic.c"]
 HDRS = [HERE / "gdc_oracle.h", HERE / "gdc_fftpack.h"]
 LIB = OUT / "libgdc_oracle.so"
 LIB_REF = OUT / "libgdc_oracle_ref.so"

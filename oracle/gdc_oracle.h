@@ -51,6 +51,13 @@ int gdo_rfft_row(int n, int backward, double* x);
  * (index 0) and s2 (index 1) since the last call, with the field (0 du,
  * 1 dv, 2 dgd) and Fortran row where it occurred; resets the record. */
 void gdo_rescale_record(gdo_model* m, double* cond, int* field, int* row);
+/* The benchmark's seeded state and its noise (gdc_oracle_ic.c): the
+ * library's gdc_ic_seeded / gdc_ic_add_noise evaluated the same way, in
+ * the padded layout with ld = num_lon + 4, without the library. */
+int gdo_ic_seeded(int N, int M, unsigned long long seed, int lmax, double gd0, double gd_rms, double psi_rms,
+                  double u0, int n_mountains, double mountain_height, double mountain_radius_deg, double* u,
+                  double* v, double* gd, double* ghs);
+int gdo_ic_add_noise(int N, int M, unsigned long long seed, double sigma, double* gd);
 /* The oracle's correctly rounded sum (exposed for its self-test). */
 double gdo_fsum(const double* x, int n);
 

@@ -40,6 +40,11 @@ def lib(kind: str = "exact") -> ctypes.CDLL:
         L.gdo_set_fft.argtypes = [vp, i]
         L.gdo_set_fft.restype = i
         L.gdo_rescale_record.argtypes = [vp, dp, ip, ip]
+        ull, d = ctypes.c_ulonglong, ctypes.c_double
+        L.gdo_ic_seeded.argtypes = [i, i, ull, i, d, d, d, d, i, d, d, dp, dp, dp, dp]
+        L.gdo_ic_seeded.restype = i
+        L.gdo_ic_add_noise.argtypes = [i, i, ull, d, dp]
+        L.gdo_ic_add_noise.restype = i
         L.gdo_rfft_row.argtypes = [i, i, dp]
         L.gdo_rfft_row.restype = i
         L.gdo_fsum.argtypes = [dp, i]
@@ -78,6 +83,28 @@ def fsum(x) -> float:
     """The oracle's correctly rounded summation."""
     a = np.ascontiguousarray(x, dtype=np.float64)
     return lib().gdo_fsum(_ptr(a), len(a))
+
+
+G = 9.80616
+
+
+def ic_seeded(N, M, seed=0, lmax=6, gd0=8000 * G, gd_rms=100 * G, psi_rms=1.0e7, u0=0.0, n_mountains=0,
+              mountain_height=2000.0, mountain_radius_deg=20.0):
+    """The benchmark's seeded state (padded layout), built by the oracle
+    without the product library; bitwise the library's gdc_ic_seeded."""
+    u, v, gd, ghs = _pad(M, N), _pad(M - 1, N), _pad(M, N), _pad(M, N)
+    rc = lib("exact").gdo_ic_seeded(N, M, seed, lmax, gd0, gd_rms, psi_rms, u0, n_mountains, mountain_height,
+                                    mountain_radius_deg, _ptr(u), _ptr(v), _ptr(gd), _ptr(ghs))
+    if rc:
+        raise ValueError("gdo_ic_seeded: invalid arguments")
+    return u, v, gd, ghs
+
+
+def ic_add_noise(gd, N, M, seed, sigma):
+    """N(0, sigma) noise on gd's interior, in place (gdc_ic_add_noise's draws)."""
+    if lib("exact").gdo_ic_add_noise(N, M, seed, sigma, _ptr(gd)):
+        raise ValueError("gdo_ic_add_noise: invalid arguments")
+    return gd
 
 
 def _pad(rows, N):

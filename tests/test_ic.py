@@ -124,3 +124,41 @@ def test_oracle_propagates_sw_wave_at_its_phase_speed():
     assert abs(np.linalg.norm(f1[:, K]) / np.linalg.norm(f0[:, K]) - 1) < 0.25
     f1[:, K] = 0
     assert np.linalg.norm(np.fft.irfft(f1, n=N, axis=1)) < 0.05 * np.linalg.norm(h1)
+
+
+def test_oracle_seeded_state_is_the_library_state(native):
+    """The oracle's copy of the seeded-state definition (used where the
+    product library must not be loaded: the benchmark's reference arm) is
+    bitwise the library's, noise included."""
+    from oracle import oracle as O
+    cases = [(360, 181, {}), (180, 91, dict(seed=3)),
+             (72, 37, dict(seed=5, lmax=12, n_mountains=3, u0=20.0)),
+             (144, 73, dict(lmax=0, gd_rms=0.0, psi_rms=0.0, u0=20.0, n_mountains=3, gd0=5960 * gdc.G))]
+    for N, M, kw in cases:
+        a, b = gdc.ic_seeded(N, M, **kw), O.ic_seeded(N, M, **kw)
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y), (N, M)
+        g1 = gdc.ic_add_noise(a[2].copy(), N, M, seed=1001, sigma=gdc.G)
+        g2 = O.ic_add_noise(b[2].copy(), N, M, 1001, gdc.G)
+        assert np.array_equal(g1, g2)
+
+
+def test_reference_arm_worker_runs_without_the_product_library():
+    """bench.py's reference arm: a worker process builds its members from
+    the oracle alone, advances them, and reports that libgdc.so is not
+    mapped in it."""
+    import multiprocessing as mp
+    import bench
+    ctx = mp.get_context("spawn")
+    a, b = ctx.Pipe()
+    task = dict(N=72, M=37, dt=1200.0, nsteps=3, cutoff=[3, 3], seed=1000)
+    pr = ctx.Process(target=bench._ref_worker, args=(b, [str(bench.ROOT)], [task]))
+    pr.start()
+    tag, mapped = a.recv()
+    assert tag == "ready" and mapped is False
+    a.send(5)  # more steps than the member's length: it stops at 3
+    done, nan = a.recv()
+    assert done == 72 * 37 * 3 and nan == 0
+    a.send(None)
+    pr.join(timeout=60)
+    assert pr.exitcode == 0
