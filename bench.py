@@ -186,9 +186,7 @@ def time_batch(gdc, torch, members, steps, warmup, precision, ts):
     b.step(warmup)
     b.sync()
     gpt = sum(m["N"] * m["M"] * min(steps, m["nsteps"]) for m in members)
-    # per predict_correct: 3 stage launches, beta, final; 6 + 2 calls per
-    # csp2 step; then diag + diag_finalize
-    launches_per_step = 5 * (6 + 2) + 2
+    launches_per_step = step_launches()
     active_steps = sum(min(steps, m["nsteps"]) for m in members)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
@@ -201,6 +199,31 @@ def time_batch(gdc, torch, members, steps, warmup, precision, ts):
     nan = [b.info(i)[2] for i in ids]
     b.close()
     return ms, gpt, launches_per_step * max(min(steps, m["nsteps"]) for m in members), active_steps, nan
+
+
+SUBCYCLES = 6
+
+
+def step_launches(subcycles=SUBCYCLES, fused=True):
+    """Kernel launches of one csp2 model step: per predict_correct 3 stage
+    launches and beta, the final update of the step's last predict_correct
+    (the others are formed by the next one's first stage when fused), then
+    diag + diag_finalize."""
+    pcs = subcycles + 2
+    return 4 * pcs + (1 if fused else pcs) + 2
+
+
+def stage_words_per_launch(subcycles=SUBCYCLES, fused=True):
+    """Algorithmic prognostic words per grid point of a stage launch, mean
+    over a step: predict 1 reads the level and ghs, writes S1 (7); with the
+    previous final update fused it also reads that update's base level and
+    T_new and writes the level instead of reading it (13); predict 2 reads
+    S1, the base level and ghs, writes T_old and S2 (13); correct reads S2,
+    ghs and T_old, writes T_new (10).  FP32 compensation words are not
+    counted."""
+    pcs = subcycles + 2
+    s1 = 7 + (pcs - 1) * (13 if fused else 7)
+    return (s1 + 13 * pcs + 10 * pcs) / (3 * pcs)
 
 
 def e2e_batch(gdc, torch, members, steps, precision):
@@ -483,12 +506,13 @@ def run_ours(args, rank, world, dist):
     if rank != 0:
         return
     beside = beside_path(gdc, torch)
-    # Roofline of the dominant kernel (the fused stage kernel): algorithmic
-    # bytes per launch = 10 prognostic words per grid point (stages read+write
-    # 7, 13 and 10 words: 30 over 3 launches) x 4 bytes x active points.
+    # Roofline of the dominant kernel (the stage kernel): algorithmic bytes
+    # per launch = the mean prognostic words per grid point of a stage launch
+    # (stage_words_per_launch) x 4 bytes x active points.
     cells = sum(m["N"] * m["M"] for m in members)
     stage_ms = prof_ms[0] / max(prof_n[0], 1)
-    stage_bytes = 10 * 4 * cells
+    stage_words = stage_words_per_launch()
+    stage_bytes = stage_words * 4 * cells
     achieved = stage_bytes / (stage_ms / 1e3) / 1e9
     hbm = pk.get("hbm_gbs")
     peak_src = "measured" if hbm else "fallback"
@@ -517,8 +541,11 @@ def run_ours(args, rank, world, dist):
                      "traffic": stage_traffic(), "traffic_unit": "bytes per launch (ncu, mean of one predict_correct)",
                      "kernel": "stage_kernel<float, pass, 0, 16, 64>", "peak_source": peak_src,
                      "stage_ms_per_launch": stage_ms, "bytes_per_launch": stage_bytes,
-                     "kernel_ms": {"stage": prof_ms[0], "final": prof_ms[1], "diag": prof_ms[2]},
-                     "kernel_launches": {"stage": prof_n[0], "final": prof_n[1], "diag": prof_n[2]},
+                     "words_per_point_per_launch": stage_words,
+                     "kernel_ms": {"stage": prof_ms[0], "final": prof_ms[1], "beta": prof_ms[4],
+                                   "diag": prof_ms[2]},
+                     "kernel_launches": {"stage": prof_n[0], "final": prof_n[1], "beta": prof_n[4],
+                                         "diag": prof_n[2]},
                      "whole_step_frac": (gpt / (ms / 1e3)) * algo_bytes / 1e9 / hbm},
         "plain_fp64": {"value": plain["value"], "unit": "grid-pt-steps/s",
                        "config": "360x181 dt 240 s, 360 steps, FP64, one member",

@@ -133,6 +133,7 @@ struct BatchIface {
   virtual int diag(int id, double* m, double* e, double* b) = 0;
   virtual int active(int* n) = 0;
   virtual int set_tile(int r, int c) = 0;
+  virtual int set_schedule(int split_rows, int fuse_final) = 0;
   virtual int autotune(int* r, int* c, double* ms) = 0;
   virtual int profile(int n, double* ms, long long* launches) = 0;
   virtual int set_stream(void* s) = 0;
@@ -836,6 +837,15 @@ class Batch final : public BatchIface {
     return GDC_OK;
   }
 
+  int set_schedule(int split, int fuse) override {
+    if (split < -1 || split > 1 || fuse < 0 || fuse > 1)
+      return fail(GDC_E_CONFIG, "set_schedule: split_rows must be -1, 0 or 1 and fuse_final 0 or 1");
+    split_mode = split;
+    fuse_final = fuse != 0;
+    dirty = true;
+    return GDC_OK;
+  }
+
   int set_stream(void* s) override {
     sync_stream();
     stream = s ? (cudaStream_t)s : own_stream;
@@ -887,7 +897,7 @@ class Batch final : public BatchIface {
   }
 
   int profile(int n, double* ms, long long* launches) override {
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < 5; ++k) {
       ms[k] = 0;
       launches[k] = 0;
     }
@@ -1035,6 +1045,8 @@ class Batch final : public BatchIface {
   // work) or when the batch has few tiles per SM (the row tasks are then the
   // critical path); otherwise one task per row stages the row once.
   bool split_rows = sizeof(T) == 8;
+  int split_mode = -1;     // -1 automatic (above), 0 whole rows, 1 split by field
+  bool fuse_final = true;  // predict_correct's update formed in the next one's first stage
   int num_sms = 152;
   // With strips, the whole-row tasks run on a second stream, concurrently
   // with the strips over the ordinary rows.
@@ -1214,7 +1226,7 @@ class Batch final : public BatchIface {
         const long long cols = strips ? (recs[s].N + kStripCols - 1) / kStripCols : (recs[s].N + tile_c - 1) / tile_c;
         ntiles += cols * ((recs[s].M + tile_r - 1) / tile_r);
       }
-      split_rows = sizeof(T) == 8 || ntiles < 8LL * num_sms;
+      split_rows = split_mode >= 0 ? split_mode == 1 : (sizeof(T) == 8 || ntiles < 8LL * num_sms);
     }
     for (int s = 0; s < kSlots; ++s) {
       if (!recs[s].used || !recs[s].active) continue;
@@ -1367,7 +1379,7 @@ class Batch final : public BatchIface {
                             beta_mode, stream);
     if (pr) {
       cudaEventRecord(e1, stream);
-      pr->push_back(Prof{1, e0, e1});
+      pr->push_back(Prof{4, e0, e1});
     }
     return rc ? fail(rc, "beta launch failed") : GDC_OK;
   }
@@ -1386,13 +1398,32 @@ class Batch final : public BatchIface {
     return rc ? fail(rc, "final-update launch failed") : GDC_OK;
   }
 
+  // A predict_correct's final update not yet launched: level `out` =
+  // `base` + time_step_size(pass) * beta * T_new, left for the next
+  // predict_correct's first stage to form (StageArgs::fuse).
+  struct PendingFinal {
+    bool valid = false;
+    int base = -1, pass = 0;
+  };
+  bool fusable() const { return fuse_final && !strips && !weno(); }
+
   // One predict_correct call (src/dycore_mod.F90:754-792) from level o to n.
-  int predict_correct(int pass, int o, int n, std::vector<Prof>* pr) {
+  // `in`: the previous call's pending final update, formed here by the
+  // first stage (level o is its output); `out`: when given, this call's
+  // final update is left pending instead of launched.
+  int predict_correct(int pass, int o, int n, const PendingFinal* in, PendingFinal* out, std::vector<Prof>* pr) {
+    const PendingFinal prev = in ? *in : PendingFinal();
     StageArgs a = base_args(pass);
     a.in_slot = o;
     a.base_slot = o;
     a.out_slot = SL_SA;
-    if (int rc = run_stage(a, pr)) return rc;  // predict 1
+    if (prev.valid) {
+      a.fuse = 1;
+      a.fin_base = prev.base;
+      a.fin_pass = prev.pass;
+      a.fin_h_scale = 1.0;
+    }
+    if (int rc = run_stage(a, pr)) return rc;  // (final of the previous call +) predict 1
     a = base_args(pass);
     a.in_slot = SL_SA;
     a.base_slot = o;
@@ -1406,6 +1437,12 @@ class Batch final : public BatchIface {
     a.do_ip = 1;
     if (int rc = run_stage(a, pr)) return rc;  // correct
     if (int rc = run_beta(0, pr)) return rc;   // beta
+    if (out) {
+      out->valid = true;
+      out->base = o;
+      out->pass = pass;
+      return GDC_OK;
+    }
     FinalArgs f;
     f.base_slot = o;
     f.out_slot = n;
@@ -1483,18 +1520,22 @@ class Batch final : public BatchIface {
   int enqueue_step(std::vector<Prof>* pr) {
     int rc = GDC_OK;
     if (P.split_scheme == GDC_SPLIT_CSP2) {
-      // csp2_splitting (src/dycore_mod.F90:671-687)
+      // csp2_splitting (src/dycore_mod.F90:671-687).  Every final update but
+      // the step's last (diag_run reads the step's new level) is formed by
+      // the next predict_correct's first stage when fusable.
+      PendingFinal pend;
+      PendingFinal* pp = fusable() ? &pend : nullptr;
       int t1 = SL_L0, t2 = old_;
-      rc = predict_correct(kSlowPass, old_, t1, pr);
+      rc = predict_correct(kSlowPass, old_, t1, nullptr, pp, pr);
       for (int k = 0; k < P.subcycles && !rc; ++k) {
-        rc = predict_correct(kFastPass, t1, t2, pr);
+        rc = predict_correct(kFastPass, t1, t2, pp, pp, pr);
         std::swap(t1, t2);
       }
-      if (!rc) rc = predict_correct(kSlowPass, t1, new_, pr);
+      if (!rc) rc = predict_correct(kSlowPass, t1, new_, pp, nullptr, pr);
     } else if (P.split_scheme == GDC_SPLIT_ISP) {
       rc = isp(pr);
     } else {
-      rc = predict_correct(kAllPass, old_, new_, pr);
+      rc = predict_correct(kAllPass, old_, new_, nullptr, nullptr, pr);
     }
     if (rc) return rc;
     if (P.use_diffusion) {
@@ -1731,6 +1772,9 @@ int gdc_batch_diag(gdc_batch* b, int id, double* m, double* e, double* beta) {
 }
 int gdc_batch_active(gdc_batch* b, int* n) { return (b && n) ? b->impl->active(n) : GDC_E_CONFIG; }
 int gdc_batch_set_tile(gdc_batch* b, int r, int c) { return b ? b->impl->set_tile(r, c) : GDC_E_CONFIG; }
+int gdc_batch_set_schedule(gdc_batch* b, int split_rows, int fuse_final) {
+  return b ? b->impl->set_schedule(split_rows, fuse_final) : GDC_E_CONFIG;
+}
 int gdc_batch_history(gdc_batch* b, int member_id, double* u_a, double* v_a, double* gh, double* div, double* vor,
                       int ld) {
   return b ? b->impl->history(member_id, u_a, v_a, gh, div, vor, ld) : GDC_E_CONFIG;

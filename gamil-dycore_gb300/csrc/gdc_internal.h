@@ -235,6 +235,14 @@ struct StageArgs {
   double rescale_rtol;               // gdc_params::filter_rescale_rtol
   int* uvslot;                       // per member: slot whose u, v are given (-1 none)
   int form;                          // UpdateForm, set by the launchers
+  // Fused final update (predict form only): the input level in_slot is
+  // first formed, for every point the block stages, as the previous
+  // predict_correct's update in_slot = fin_base + pcdt[fin_pass] *
+  // fin_h_scale * beta * T_new (compensated in FP32, as final_kernel), and
+  // the block writes it for its own points.
+  int fuse;
+  int fin_base, fin_pass;
+  double fin_h_scale;
 };
 
 // Warp strips: output columns per warp (lanes 1..30 of the 32), and the

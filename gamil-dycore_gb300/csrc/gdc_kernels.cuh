@@ -247,9 +247,12 @@ __device__ __forceinline__ void cp_async16(T* smem, const T* gmem, bool valid) {
 // row interiors (columns i0 .. i0+vcols-1, never wrapping) go 16 bytes at a
 // time; the halo columns i0-1, i0+vcols, i0+vcols+1 element by element.
 // Requires num_lon and i0 to be multiples of VEC (checked at admission).
+// With `tend` (a fused final update), the tendencies of the level's update
+// are staged into the ig, u and v areas (free until tile_derive).
 template <typename T, int R, int W>
 __device__ void tile_issue(const MemberDev<T>& md, const T* __restrict__ gd, const T* __restrict__ iu,
-                           const T* __restrict__ iv, Tile<T, R, W>& t, bool given = false, bool want_ghs = true) {
+                           const T* __restrict__ iv, Tile<T, R, W>& t, bool given = false, bool want_ghs = true,
+                           T* const* tend = nullptr) {
   using TL = Tile<T, R, W>;
   constexpr int VEC = TL::VEC, NCH = W / VEC;
   const int N = md.N, M = md.M, Mh = md.Mh;
@@ -272,6 +275,11 @@ __device__ void tile_issue(const MemberDev<T>& md, const T* __restrict__ gd, con
       cp_async16(&t.u[dp], md.given_u + o, vf);
       cp_async16(&t.v[dp], md.given_v + (vh ? o : 0), vh);
     }
+    if (tend) {
+      cp_async16(&t.ig[dp], tend[F_GD] + o, vf);
+      cp_async16(&t.u[dp], tend[F_IU] + o, vf);
+      cp_async16(&t.v[dp], tend[F_IV] + (vh ? o : 0), vh);
+    }
   }
   // halo columns
   for (int q = threadIdx.x; q < TL::ROWS * 3; q += kThreads) {
@@ -292,6 +300,11 @@ __device__ void tile_issue(const MemberDev<T>& md, const T* __restrict__ gd, con
       cp_async(&t.u[dp], md.given_u + o, vf);
       cp_async(&t.v[dp], md.given_v + (vh ? o : 0), vh);
     }
+    if (tend) {
+      cp_async(&t.ig[dp], tend[F_GD] + o, vf);
+      cp_async(&t.u[dp], tend[F_IU] + o, vf);
+      cp_async(&t.v[dp], tend[F_IV] + (vh ? o : 0), vh);
+    }
   }
   (void)nfield;
   // coefficient records of rows j0-1..j0+R (records exist for rows -1..M)
@@ -302,6 +315,61 @@ __device__ void tile_issue(const MemberDev<T>& md, const T* __restrict__ gd, con
     if (j > M) continue;  // beyond a partial tile: never read
     cp_async16(&t.rc[lr * kRecWords + k * VEC], md.rowc + (size_t)(j + 1) * kRecWords + k * VEC, true);
   }
+}
+
+// The fused final update (StageArgs::fuse): after the copies, every staged
+// position of gd, iap u, iap v becomes the previous predict_correct's new
+// level, fin_base + h T_new with h = pcdt[fin_pass] * fin_h_scale * beta --
+// in FP32 with its compensation word, TwoSum of lo + h T onto hi, exactly
+// as final_kernel forms it -- and the block writes the level (and its
+// compensation words) for the points it owns: rows 1..vrows, columns
+// 1..vcols of the tile, of the fields in `own_fields` (bit f for field f).
+template <typename T, int R, int W>
+__device__ void tile_combine(const MemberDev<T>& md, const StageArgs& a, int member, Tile<T, R, W>& t,
+                             int own_fields) {
+  using TL = Tile<T, R, W>;
+  const int N = md.N, M = md.M, Mh = md.Mh;
+  const T h = T(md.pcdt[a.fin_pass] * a.fin_h_scale * a.beta[member]);
+  T* const* lo = md.lo[a.fin_base];
+  T* const* out = md.st[a.in_slot];
+  T* const* olo = md.lo[a.in_slot];
+  constexpr int CW = W + 3;  // staged columns i0-1 .. i0+W+1
+  cp_async_wait_all();
+  __syncthreads();
+  for (int q = threadIdx.x; q < TL::ROWS * CW; q += kThreads) {
+    const int rr = q / CW, cc = q - rr * CW;
+    if (rr > t.vrows + 2 || cc > t.vcols + 2) continue;  // not staged
+    const int j = t.j0 - 1 + rr;
+    if (j < 0 || j >= M) continue;  // off the sphere: zero, as staged
+    int i = t.i0 - 1 + cc;
+    i = i < 0 ? i + N : (i >= N ? i - N : i);
+    const int p = TL::pos(rr, cc);
+    const bool own = rr >= 1 && rr <= t.vrows && cc >= 1 && cc <= t.vcols;
+    const size_t o = (size_t)j * N + i;
+    T* hi[3] = {t.gd, t.iu, t.iv};
+    const T* tt[3] = {t.ig, t.u, t.v};
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      if (f == F_IV && j >= Mh) continue;
+      const T x = hi[f][p];
+      if (lo[f]) {
+        const T y = lo[f][o] + h * tt[f][p];
+        const T sum = x + y;
+        const T bp = sum - x;
+        const T e = (x - (sum - bp)) + (y - bp);
+        hi[f][p] = sum;
+        if (own && (own_fields >> f & 1)) {
+          out[f][o] = sum;
+          olo[f][o] = e;
+        }
+      } else {
+        const T sum = x + h * tt[f][p];
+        hi[f][p] = sum;
+        if (own && (own_fields >> f & 1)) out[f][o] = sum;
+      }
+    }
+  }
+  __syncthreads();
 }
 
 // After the copies: iap gd, then u on full rows j0..j0+R (local 1..R+1;
@@ -508,6 +576,32 @@ struct Emit {
   Acc<T> ip1, ip2;
   __device__ Emit(const MemberDev<T>& m, const StageArgs& s, T h_) : md(m), a(s), h(h_), s2(T(s.scale2)) {}
 
+  // One point's terms of predict_correct's inner products (beta_mode 0).
+  // FP64 adds prev*val*w and val*val*w to <T_old, T_new> and <T_new, T_new>
+  // as the reference does (double-double: the oracle's exact sums).  FP32
+  // forms d = <T_old - T_new, T_new> in place of <T_old, T_new>, so that
+  // beta = 1 + d / <T_new, T_new> (the same ratio): beta - 1 is carried by
+  // d itself instead of by the difference of two nearly equal sums, and
+  // plain float sums local to the thread suffice; ip_flush folds them into
+  // the compensated block sums.
+  T l1 = T(0), l2 = T(0);
+  __device__ __forceinline__ void ip_point(T prev, T val, T w) {
+    if constexpr (sizeof(T) == 4) {
+      l1 += (prev - val) * val * w;
+      l2 += val * val * w;
+    } else {
+      ip1.add(prev * val * w);
+      ip2.add(val * val * w);
+    }
+  }
+  __device__ __forceinline__ void ip_flush() {
+    if constexpr (sizeof(T) == 4) {
+      ip1.add(l1);
+      ip2.add(l2);
+      l1 = l2 = T(0);
+    }
+  }
+
   __device__ void put(int f, size_t o, T val, T wcos, T base, T prev) {
     if (a.taccum >= 0) {
       // add_data(tend, accum_fast_tend), src/dycore_mod.F90:721
@@ -525,8 +619,12 @@ struct Emit {
     if (a.out_slot >= 0) md.st[a.out_slot][f][o] = base + h * val;
     if (a.do_ip) {
       // inner_product_tend_tend / _tend_state, src/types_mod.F90:347-397
-      ip1.add(prev * val * wcos);
-      ip2.add(val * val * wcos);
+      if (a.beta_mode == 0) {
+        ip_point(prev, val, wcos);
+      } else {
+        ip1.add(prev * val * wcos);
+        ip2.add(val * val * wcos);
+      }
     }
   }
   // Operands read straight from global memory (row tasks, isp modes).
@@ -810,8 +908,9 @@ __device__ __forceinline__ void bulk_tile(const MemberDev<T>& md, const StageArg
   static_assert(RPT * kThreads == R * W, "a tile is a whole number of rows per thread");
   const int N = md.N;
   TL t = carve<T, R, W>(staging, w.j0, w.i0, w.rows, w.cols);
+  const bool fuse = UF == UF_PREDICT_IN && a.fuse;
   // The slow pass (advection) reads no ghs, the fast pass no v.
-  tile_issue(md, gd_in, iu_in, iv_in, t, given, PASS != kSlowPass);
+  tile_issue(md, gd_in, iu_in, iv_in, t, given, PASS != kSlowPass, fuse ? md.td[TS_NEW] : nullptr);
   const int c = threadIdx.x % W, r0 = (threadIdx.x / W) * RPT;
   const bool cval = c < w.cols;
   const int ob = (w.j0 + r0) * N + w.i0 + c;  // the thread's first point
@@ -825,6 +924,7 @@ __device__ __forceinline__ void bulk_tile(const MemberDev<T>& md, const StageArg
 #pragma unroll
       for (int f = 0; f < 3; ++f) pre[k][f] = (cval && r0 + k < w.rows) ? src[f][ob + k * N] : T(0);
   }
+  if (fuse) tile_combine(md, a, w.member, t, 7);
   tile_derive(md, t, false, given, PASS != kFastPass);
   T* dst[3] = {nullptr, nullptr, nullptr};
   T* tdst[3] = {nullptr, nullptr, nullptr};
@@ -866,20 +966,18 @@ __device__ __forceinline__ void bulk_tile(const MemberDev<T>& md, const StageArg
       // of terms as Emit::put
       const T wf = t.cf(TF_COS, j), wh = t.ch(TH_COS, j);
       tdst[F_IU][o] = du;
-      em.ip1.add(pre[k][F_IU] * du * wf);
-      em.ip2.add(du * du * wf);
+      em.ip_point(pre[k][F_IU], du, wf);
       tdst[F_IV][o] = dv;
-      em.ip1.add(pre[k][F_IV] * dv * wh);
-      em.ip2.add(dv * dv * wh);
+      em.ip_point(pre[k][F_IV], dv, wh);
       tdst[F_GD][o] = dg;
-      em.ip1.add(pre[k][F_GD] * dg * wf);
-      em.ip2.add(dg * dg * wf);
+      em.ip_point(pre[k][F_GD], dg, wf);
     } else {
       em.put(F_IU, o, du, t.cf(TF_COS, j), em.base_of(F_IU, o), em.prev_of(F_IU, o));
       em.put(F_IV, o, dv, t.ch(TH_COS, j), em.base_of(F_IV, o), em.prev_of(F_IV, o));
       em.put(F_GD, o, dg, t.cf(TF_COS, j), em.base_of(F_GD, o), em.prev_of(F_GD, o));
     }
   }
+  em.ip_flush();
 }
 
 // ------------------------------------------------- column pairs (FP32)
@@ -951,7 +1049,8 @@ __device__ __forceinline__ void bulk_tile_pair(const MemberDev<float>& md, const
   static_assert(RPT * kThreads == R * PW, "a tile is a whole number of pair rows per thread");
   const int N = md.N;
   TL t = carve<T, R, W>(staging, w.j0, w.i0, w.rows, w.cols);
-  tile_issue(md, gd_in, iu_in, iv_in, t, given, PASS != kSlowPass);
+  const bool fuse = UF == UF_PREDICT_IN && a.fuse;
+  tile_issue(md, gd_in, iu_in, iv_in, t, given, PASS != kSlowPass, fuse ? md.td[TS_NEW] : nullptr);
   const int c = 2 * (threadIdx.x % PW), r0 = (threadIdx.x / PW) * RPT;
   const bool cval = c < w.cols;
   const int ob = (w.j0 + r0) * N + w.i0 + c;
@@ -963,6 +1062,7 @@ __device__ __forceinline__ void bulk_tile_pair(const MemberDev<float>& md, const
 #pragma unroll
       for (int f = 0; f < 3; ++f) pre[k][f] = (cval && r0 + k < w.rows) ? ld2(src[f] + ob + k * N) : F2(0.0f);
   }
+  if (fuse) tile_combine(md, a, w.member, t, 7);
   tile_derive(md, t, false, given, PASS != kFastPass);
   T* dst[3] = {nullptr, nullptr, nullptr};
   T* tdst[3] = {nullptr, nullptr, nullptr};
@@ -1004,18 +1104,12 @@ __device__ __forceinline__ void bulk_tile_pair(const MemberDev<float>& md, const
       st2(tdst[F_IV] + o, dv);
       st2(tdst[F_GD] + o, dg);
       // the scalar path's order of terms, point by point
-      em.ip1.add(pre[k][F_IU].x * du.x * wf);
-      em.ip2.add(du.x * du.x * wf);
-      em.ip1.add(pre[k][F_IV].x * dv.x * wh);
-      em.ip2.add(dv.x * dv.x * wh);
-      em.ip1.add(pre[k][F_GD].x * dg.x * wf);
-      em.ip2.add(dg.x * dg.x * wf);
-      em.ip1.add(pre[k][F_IU].y * du.y * wf);
-      em.ip2.add(du.y * du.y * wf);
-      em.ip1.add(pre[k][F_IV].y * dv.y * wh);
-      em.ip2.add(dv.y * dv.y * wh);
-      em.ip1.add(pre[k][F_GD].y * dg.y * wf);
-      em.ip2.add(dg.y * dg.y * wf);
+      em.ip_point(pre[k][F_IU].x, du.x, wf);
+      em.ip_point(pre[k][F_IV].x, dv.x, wh);
+      em.ip_point(pre[k][F_GD].x, dg.x, wf);
+      em.ip_point(pre[k][F_IU].y, du.y, wf);
+      em.ip_point(pre[k][F_IV].y, dv.y, wh);
+      em.ip_point(pre[k][F_GD].y, dg.y, wf);
     } else {
       const T wf = t.cf(TF_COS, j), wh = t.ch(TH_COS, j);
       em.put(F_IU, o, du.x, wf, em.base_of(F_IU, o), em.prev_of(F_IU, o));
@@ -1026,6 +1120,7 @@ __device__ __forceinline__ void bulk_tile_pair(const MemberDev<float>& md, const
       em.put(F_GD, o + 1, dg.y, wf, em.base_of(F_GD, o + 1), em.prev_of(F_GD, o + 1));
     }
   }
+  em.ip_flush();
 }
 
 // The bulk tile of a stage: column pairs for FP32 tiles whose pair count
@@ -1287,20 +1382,18 @@ __device__ void strip_warp(const MemberDev<T>& md, const WorkItem& w, const Stag
         dst[F_GD][o] = pre[F_GD] + h * dg;
       } else if (UF == UF_CORRECT) {
         tdst[F_IU][o] = du;
-        em.ip1.add(pre[F_IU] * du * wf);
-        em.ip2.add(du * du * wf);
+        em.ip_point(pre[F_IU], du, wf);
         tdst[F_IV][o] = dv;
-        em.ip1.add(pre[F_IV] * dv * wh);
-        em.ip2.add(dv * dv * wh);
+        em.ip_point(pre[F_IV], dv, wh);
         tdst[F_GD][o] = dg;
-        em.ip1.add(pre[F_GD] * dg * wf);
-        em.ip2.add(dg * dg * wf);
+        em.ip_point(pre[F_GD], dg, wf);
       } else {
         em.put(F_IU, o, du, wf, em.base_of(F_IU, o), em.prev_of(F_IU, o));
         em.put(F_IV, o, dv, wh, em.base_of(F_IV, o), em.prev_of(F_IV, o));
         em.put(F_GD, o, dg, wf, em.base_of(F_GD, o), em.prev_of(F_GD, o));
       }
     }
+    em.ip_flush();  // one row of the strip
     cos_prev = wh;
     rec = rec_next;
     // Advance the window by one row: derive row j+2 (raw p1, with the iap
@@ -1383,6 +1476,7 @@ __device__ void row_tail(const MemberDev<T>& md, const StageArgs& a, Emit<T>& em
     else
       em.put(f, o, x[i], w, em.base_of(f, o), em.prev_of(f, o));
   }
+  em.ip_flush();
 }
 
 template <typename T>
@@ -1405,17 +1499,24 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
   // it to shared memory cost a barrier per block.
   const MemberDev<T>& md = mems[w.member];
   const int N = md.N, M = md.M, Mh = md.Mh;
-  const T* gd_in = md.st[a.in_slot][F_GD];
-  const T* iu_in = md.st[a.in_slot][F_IU];
-  const T* iv_in = md.st[a.in_slot][F_IV];
+  // A fused final update stages its base level (and forms in_slot from it).
+  const bool fuse = a.fuse && a.form == UF_PREDICT_IN;
+  const int src_slot = fuse ? a.fin_base : a.in_slot;
+  const T* gd_in = md.st[src_slot][F_GD];
+  const T* iu_in = md.st[src_slot][F_IU];
+  const T* iv_in = md.st[src_slot][F_IV];
   const double hstep = md.pcdt[PASS] * a.h_scale;
   Emit<T> em(md, a, T(hstep));
   const T ub_lon = T(a.ub_lon), ub_lat = T(a.ub_lat);
   // u, v supplied with this level (initial condition, diffusion): used as
-  // given, as the reference's space_operators reads state%u / state%v.
-  const bool given = a.uvslot && a.uvslot[w.member] == a.in_slot;
-  if (a.uvslot && a.out_slot >= 0 && threadIdx.x == 0 && a.uvslot[w.member] == a.out_slot)
-    a.uvslot[w.member] = -1;  // level overwritten: u, v derived from now on
+  // given, as the reference's space_operators reads state%u / state%v.  A
+  // level formed by a fused update is never given: u, v derived from now on.
+  const bool given = !fuse && a.uvslot && a.uvslot[w.member] == a.in_slot;
+  if (a.uvslot && threadIdx.x == 0) {
+    const int g = a.uvslot[w.member];
+    if ((a.out_slot >= 0 && g == a.out_slot) || (fuse && g == a.in_slot))
+      a.uvslot[w.member] = -1;  // level overwritten: u, v derived from now on
+  }
 
   if (w.kind == 0) {
     // ---------------- bulk tile: rows j0..j0+R-1 are ordinary rows
@@ -1450,7 +1551,8 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
       const int vw = min(kRowChunk, N - c0);
       TR t = carve<T, 1, kRowChunk>(staging, j, c0, 1, vw);
       __syncthreads();
-      tile_issue(md, gd_in, iu_in, iv_in, t, given, PASS != kSlowPass);
+      tile_issue(md, gd_in, iu_in, iv_in, t, given, PASS != kSlowPass, fuse ? md.td[TS_NEW] : nullptr);
+      if (fuse) tile_combine(md, a, w.member, t, f < 0 ? 7 : (1 << f));
       tile_derive(md, t, false, given, PASS != kFastPass);
       for (int c = threadIdx.x; c < vw; c += blockDim.x) {
         const int p = TR::pos(1, c + 1);
@@ -1544,7 +1646,14 @@ __device__ void member_beta(const MemberDev<T>& md, int s, const double* partial
   const double ip1 = block_value(a1, red);
   const double ip2 = block_value(a2, red);
   if (threadIdx.x == 0) {
-    double b = (qcon && ip1 != 0.0 && ip2 != 0.0) ? ip1 / ip2 : 1.0;
+    double b;
+    if (sizeof(T) == 4 && beta_mode == 0) {
+      // FP32 partials carry d = <T_old - T_new, T_new> (Emit::ip_point):
+      // <T_old, T_new> = ip2 + d and beta = 1 + d / ip2.
+      b = (qcon && ip2 + ip1 != 0.0 && ip2 != 0.0) ? 1.0 + ip1 / ip2 : 1.0;
+    } else {
+      b = (qcon && ip1 != 0.0 && ip2 != 0.0) ? ip1 / ip2 : 1.0;
+    }
     if (beta_mode == 1) b = b * 4.0 / md.dt;
     beta[s] = b;
   }

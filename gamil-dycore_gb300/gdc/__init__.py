@@ -153,6 +153,7 @@ def lib() -> ctypes.CDLL:
             "gdc_batch_diag": (ctypes.c_int, [vp, ctypes.c_int, dp, dp, dp]),
             "gdc_batch_active": (ctypes.c_int, [vp, ip]),
             "gdc_batch_set_tile": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
+            "gdc_batch_set_schedule": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
             "gdc_batch_checkpoint": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_char_p]),
             "gdc_batch_restore": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_size_t, ip]),
             "gdc_write_restart": (ctypes.c_int, [vp, ctypes.c_char_p]),
@@ -498,14 +499,19 @@ class Batch:
     def set_tile(self, rows: int, cols: int):
         self._check(lib().gdc_batch_set_tile(self.b, rows, cols))
 
+    def set_schedule(self, split_rows: int = -1, fuse_final: int = 1):
+        """Launch schedule: whole-row tasks split by field (-1 auto, 0, 1) and
+        the final update fused into the next stage (1) or launched (0)."""
+        self._check(lib().gdc_batch_set_schedule(self.b, split_rows, fuse_final))
+
     def autotune(self):
         r, c, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
         self._check(lib().gdc_batch_autotune(self.b, ctypes.byref(r), ctypes.byref(c), ctypes.byref(ms)))
         return r.value, c.value, ms.value
 
     def profile(self, nsteps: int):
-        ms = (ctypes.c_double * 4)()
-        n = (ctypes.c_longlong * 4)()
+        ms = (ctypes.c_double * 5)()
+        n = (ctypes.c_longlong * 5)()
         self._check(lib().gdc_batch_profile(self.b, nsteps, ms, n))
         return list(ms), list(n)
 

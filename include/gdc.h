@@ -319,13 +319,26 @@ int gdc_batch_active(gdc_batch* b, int* n_active);
  * gdc_batch_autotune times the candidates on the current members and keeps
  * the fastest; the chosen shape is returned. */
 int gdc_batch_set_tile(gdc_batch* b, int tile_rows, int tile_cols);
+/* Launch schedule of the stage kernels (a choice of how the work is
+ * split, which gdc_batch_autotune also tunes): split_rows -1 picks
+ * automatically (one task per field in FP64 and in batches with few tiles
+ * per SM, one task per row otherwise), 0 one whole-row task per pole or
+ * filtered row, 1 one task per field of such a row; fuse_final 1 (default)
+ * forms each predict_correct's final update (src/dycore_mod.F90:789-790)
+ * in the first stage of the next predict_correct of the same step instead
+ * of a launch of its own (tiles only; WENO batches and warp strips always
+ * launch it).  FP64 results are bitwise the same under every schedule;
+ * FP32 results agree to rounding (the partial sums of beta group
+ * differently). */
+int gdc_batch_set_schedule(gdc_batch* b, int split_rows, int fuse_final);
 int gdc_batch_autotune(gdc_batch* b, int* tile_rows, int* tile_cols,
                        double* best_ms_per_step);
 
 /* Per-kernel-kind device time of `nsteps` steps run launch by launch with
  * CUDA events on the batch's stream (no graph).  Kinds: 0 stage (tendency
- * + update), 1 final update, 2 diag, 3 diffusion.  ms[k] total, launches[k]
- * count.  Advances the members like gdc_batch_step. */
+ * + update, including fused final updates), 1 final update, 2 diag, 3
+ * diffusion, 4 beta.  ms[k] total, launches[k] count (5 entries each).
+ * Advances the members like gdc_batch_step. */
 int gdc_batch_profile(gdc_batch* b, int nsteps, double* ms, long long* launches);
 /* Algorithmic bytes one grid-point-step moves (the roofline numerator
  * convention: prognostic words read+written per stage, summed over a

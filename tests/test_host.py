@@ -88,3 +88,12 @@ def test_algorithmic_bytes(native):
     p.precision = gdc.FP64
     assert gdc.algorithmic_bytes_per_gpt_step(p) == (39 * 8 + 4) * 8
     assert gdc.member_bytes(p, 360, 181) > 20 * 360 * 181 * 8
+
+
+def test_driver_prints_usage_without_arguments(native):
+    """The dycore_test program (src/dycore_test.F90:15-18): no namelist
+    argument is a usage error, exit status 1, before any device work."""
+    import subprocess
+    build = __import__("build")
+    out = subprocess.run([str(build.OUT / "dycore_test")], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 1 and "Usage" in out.stdout
