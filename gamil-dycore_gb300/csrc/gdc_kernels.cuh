@@ -1579,9 +1579,15 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
       }
     }
     __syncthreads();
-    if (want_u) row_tail<T, PASS>(md, a, em, j, F_IU, xr[F_IU], cap, coefs, redT, gd_in, iu_in, iv_in, tw);
-    if (want_v) row_tail<T, PASS>(md, a, em, j, F_IV, xr[F_IV], cap, coefs, redT, gd_in, iu_in, iv_in, tw);
-    if (want_g) row_tail<T, PASS>(md, a, em, j, F_GD, xr[F_GD], cap, coefs, redT, gd_in, iu_in, iv_in, tw);
+    // The filter's weights are the input level: with a fused update, the
+    // level this block has just formed and written for its own field(s) of
+    // row j (visible to the block after the barrier above).
+    const T* wg = fuse ? md.st[a.in_slot][F_GD] : gd_in;
+    const T* wu = fuse ? md.st[a.in_slot][F_IU] : iu_in;
+    const T* wv = fuse ? md.st[a.in_slot][F_IV] : iv_in;
+    if (want_u) row_tail<T, PASS>(md, a, em, j, F_IU, xr[F_IU], cap, coefs, redT, wg, wu, wv, tw);
+    if (want_v) row_tail<T, PASS>(md, a, em, j, F_IV, xr[F_IV], cap, coefs, redT, wg, wu, wv, tw);
+    if (want_g) row_tail<T, PASS>(md, a, em, j, F_GD, xr[F_GD], cap, coefs, redT, wg, wu, wv, tw);
   }
 
   if (a.do_ip) {
