@@ -185,8 +185,11 @@ def time_batch(gdc, torch, members, steps, warmup, precision, ts):
         ids.append(b.add(m["N"], m["M"], m["dt"], warmup + m["nsteps"], *m["ic"], cutoff=m["cutoff"]))
     b.step(warmup)
     b.sync()
+    # the launch schedule picked by the batch's autotuner (restores the members)
+    b.autotune()
+    sched = b.schedule()
     gpt = sum(m["N"] * m["M"] * min(steps, m["nsteps"]) for m in members)
-    launches_per_step = step_launches()
+    launches_per_step = step_launches(fused=bool(sched["fuse_final"]))
     active_steps = sum(min(steps, m["nsteps"]) for m in members)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
@@ -198,7 +201,7 @@ def time_batch(gdc, torch, members, steps, warmup, precision, ts):
     b.sync()
     nan = [b.info(i)[2] for i in ids]
     b.close()
-    return ms, gpt, launches_per_step * max(min(steps, m["nsteps"]) for m in members), active_steps, nan
+    return ms, gpt, launches_per_step * max(min(steps, m["nsteps"]) for m in members), active_steps, nan, sched
 
 
 SUBCYCLES = 6
@@ -226,12 +229,20 @@ def stage_words_per_launch(subcycles=SUBCYCLES, fused=True):
     return (s1 + 13 * pcs + 10 * pcs) / (3 * pcs)
 
 
-def e2e_batch(gdc, torch, members, steps, precision):
+def apply_schedule(b, sched):
+    if sched:
+        b.set_tile(*sched["tile"])
+        b.set_schedule(sched["split_rows"], sched["fuse_final"])
+
+
+def e2e_batch(gdc, torch, members, steps, precision, sched=None):
     """The same job through the C ABI from host buffers: admit (H2D), step,
-    read every member's state back (D2H), all inside the timed region."""
+    read every member's state back (D2H), all inside the timed region; the
+    schedule the autotuner picked for the ensemble is set, not re-tuned."""
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     b = gdc.Batch(scheme(gdc, precision))
+    apply_schedule(b, sched)
     ids = [b.add(m["N"], m["M"], m["dt"], min(steps, m["nsteps"]), *m["ic"], cutoff=m["cutoff"]) for m in members]
     b.step(steps)
     b.sync()
@@ -244,9 +255,10 @@ def e2e_batch(gdc, torch, members, steps, precision):
     return (t1 - t0) * 1e3, gpt, h2d, d2h
 
 
-def profile_kernels(gdc, members, precision, nsteps=2):
+def profile_kernels(gdc, members, precision, nsteps=2, sched=None):
     """Per-kernel-kind device time, launch by launch with CUDA events."""
     b = gdc.Batch(scheme(gdc, precision))
+    apply_schedule(b, sched)
     for m in members:
         b.add(m["N"], m["M"], m["dt"], nsteps + 1, *m["ic"], cutoff=m["cutoff"])
     b.step(1)  # module load, attributes
@@ -494,14 +506,14 @@ def run_ours(args, rank, world, dist):
     # Warm the FP32 kernels and the FP64 plain path before anything is timed.
     barrier(dist)
     with Clocks(int(os.environ.get("LOCAL_RANK", 0))) as clk:
-        ms, gpt, launches, active_steps, nan = time_batch(gdc, torch, members, args.steps, args.warmup,
-                                                          gdc.FP32, ts)
+        ms, gpt, launches, active_steps, nan, sched = time_batch(gdc, torch, members, args.steps, args.warmup,
+                                                                 gdc.FP32, ts)
     clocks = clk.summary()
     value, ms_all = replica_value(dist, gpt, ms)
     plain = plain_fp64(gdc, torch, ts)
-    e2e_ms, e2e_gpt, h2d, d2h = e2e_batch(gdc, torch, members, args.steps, gdc.FP32)
+    e2e_ms, e2e_gpt, h2d, d2h = e2e_batch(gdc, torch, members, args.steps, gdc.FP32, sched)
     e2e_ms = reduce_max(dist, e2e_ms)
-    prof_ms, prof_n = profile_kernels(gdc, members, gdc.FP32)
+    prof_ms, prof_n = profile_kernels(gdc, members, gdc.FP32, sched=sched)
     serving = serve_sample(gdc, ts) if rank == 0 else None
     if rank != 0:
         return
@@ -511,7 +523,7 @@ def run_ours(args, rank, world, dist):
     # (stage_words_per_launch) x 4 bytes x active points.
     cells = sum(m["N"] * m["M"] for m in members)
     stage_ms = prof_ms[0] / max(prof_n[0], 1)
-    stage_words = stage_words_per_launch()
+    stage_words = stage_words_per_launch(fused=bool(sched["fuse_final"]))
     stage_bytes = stage_words * 4 * cells
     achieved = stage_bytes / (stage_ms / 1e3) / 1e9
     hbm = pk.get("hbm_gbs")
@@ -532,14 +544,18 @@ def run_ours(args, rank, world, dist):
         "dtype": "f32",
         "data": "synthetic (seeded spherical-harmonic states + per-member N(0,1 m) noise)",
         "config": dict(ENSEMBLE_CONFIG, members=len(members), grid_pt_steps=gpt,
-                       parallelism=f"replicas x{world}"),
+                       parallelism=f"replicas x{world}",
+                       schedule=f"autotuned: tiles {sched['tile'][0]}x{sched['tile'][1]}, "
+                                f"row tasks {('auto', 'whole', 'split')[sched['split_rows'] + 1]}, "
+                                f"final update {'fused' if sched['fuse_final'] else 'launched'}"),
         "clocks": clocks,
         "e2e": {"value": world * e2e_gpt / (e2e_ms / 1e3), "unit": "grid-pt-steps/s",
                 "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": stage_traffic(), "traffic_unit": "bytes per launch (ncu, mean of one predict_correct)",
-                     "kernel": "stage_kernel<float, pass, 0, 16, 64>", "peak_source": peak_src,
+                     "kernel": f"stage_kernel<float, pass, 0, {sched['tile'][0]}, {sched['tile'][1]}>",
+                     "peak_source": peak_src,
                      "stage_ms_per_launch": stage_ms, "bytes_per_launch": stage_bytes,
                      "words_per_point_per_launch": stage_words,
                      "kernel_ms": {"stage": prof_ms[0], "final": prof_ms[1], "beta": prof_ms[4],

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -134,6 +135,7 @@ struct BatchIface {
   virtual int active(int* n) = 0;
   virtual int set_tile(int r, int c) = 0;
   virtual int set_schedule(int split_rows, int fuse_final) = 0;
+  virtual int get_schedule(int* r, int* c, int* split, int* fuse) = 0;
   virtual int autotune(int* r, int* c, double* ms) = 0;
   virtual int profile(int n, double* ms, long long* launches) = 0;
   virtual int set_stream(void* s) = 0;
@@ -826,10 +828,10 @@ class Batch final : public BatchIface {
     }
     const bool st = strip_shape_supported(r, c);
     if (weno() && (r != 8 || c != 32)) return fail(GDC_E_CONFIG, "set_tile: uv_adv_scheme weno runs on 8x32 tiles");
-    if (!st && !tile_shape_supported(r, c))
+    if (!st && !tile_shape_supported(r, c, sizeof(T) == 8))
       return fail(GDC_E_CONFIG,
-                  "set_tile: supported shapes are tiles 8x32, 8x64, 4x128, 16x64 and warp strips "
-                  "8x30, 16x30, 32x30, 64x30");
+                  "set_tile: supported shapes are tiles 8x32, 8x64, 4x128, 16x64 (and 4x32 in FP64) and warp "
+                  "strips 8x30, 16x30, 32x30, 64x30");
     tile_r = r;
     tile_c = c;
     strips = st;
@@ -853,46 +855,170 @@ class Batch final : public BatchIface {
     return GDC_OK;
   }
 
-  // Times each candidate tile shape on the current members (graph replay,
-  // CUDA events) and keeps the fastest.  Advances the members.
+  // Times each candidate launch schedule -- tile shape or warp strips, the
+  // row-task split, the final update launched or fused -- on the current
+  // members (CUDA graph replay, CUDA events, the median of `reps` timed
+  // steps after warm steps) and keeps the fastest.  The members' states
+  // and all step bookkeeping are saved first and restored afterwards, so
+  // tuning advances no forecast: the members continue exactly as if it had
+  // not run.
   int autotune(int* rr, int* cc, double* best_ms) override {
-    static const int cand[][2] = {{8, 32}, {8, 64}, {16, 64}, {4, 128}, {16, 30}};
-    if (weno()) {  // one layout
-      if (int rc = set_tile(8, 32)) return rc;
-      *rr = 8;
-      *cc = 32;
+    if (dirty)
+      if (int rc = rebuild()) return rc;
+    sync_stream();
+    if (active_slots.empty() || weno()) {  // nothing to time; WENO has one layout
+      if (weno())
+        if (int rc = set_tile(8, 32)) return rc;
+      if (rr) *rr = tile_r;
+      if (cc) *cc = tile_c;
       if (best_ms) *best_ms = 0.0;
       return GDC_OK;
     }
-    double best = 1e30;
-    int br = tile_r, bc = tile_c;
-    for (auto& c : cand) {
-      if (int rc = set_tile(c[0], c[1])) return rc;
-      if (int rc = step(1)) return rc;  // build + warm
-      if (nwork == 0) break;
-      cudaEvent_t e0, e1;
-      cudaEventCreate(&e0);
-      cudaEventCreate(&e1);
-      const int reps = 3;
-      if (int rc = step(1)) return rc;
-      cudaEventRecord(e0, stream);
-      if (int rc = step(reps)) return rc;
-      cudaEventRecord(e1, stream);
-      cudaEventSynchronize(e1);
-      float ms = 0;
-      cudaEventElapsedTime(&ms, e0, e1);
-      cudaEventDestroy(e0);
-      cudaEventDestroy(e1);
-      if (ms / reps < best) {
-        best = ms / reps;
-        br = c[0];
-        bc = c[1];
+    // --- save: each active member's level (compute type, compensation
+    // words), its given u, v, the per-member device words and the host
+    // bookkeeping.
+    struct Save {
+      int slot;
+      std::vector<std::pair<T*, size_t>> fields;  // device field, elements
+      size_t off;                                  // into the scratch
+    };
+    std::vector<Save> saves;
+    size_t total = 0;
+    for (int sl : active_slots) {
+      const MemberDev<T>& d = hdesc[sl];
+      const int lvl = recs[sl].level;
+      const size_t full = (size_t)recs[sl].N * recs[sl].M, half = (size_t)recs[sl].N * (recs[sl].M - 1);
+      const size_t sz[3] = {full, full, half};
+      Save sv{sl, {}, total};
+      for (int f = 0; f < 3; ++f) {
+        sv.fields.push_back({d.st[lvl][f], sz[f]});
+        if (d.lo[lvl][f]) sv.fields.push_back({d.lo[lvl][f], sz[f]});
+      }
+      sv.fields.push_back({d.given_u, full});
+      sv.fields.push_back({d.given_v, half});
+      for (auto& f : sv.fields) total += f.second;
+      saves.push_back(sv);
+    }
+    T* scratch = nullptr;
+    if (cudaMalloc(&scratch, total * sizeof(T)) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(GDC_E_OOM, "autotune: no device memory for the members' saved states");
+    }
+    cudaError_t e = cudaSuccess;
+    for (auto& sv : saves) {
+      size_t o = sv.off;
+      for (auto& f : sv.fields) {
+        if (e == cudaSuccess)
+          e = cudaMemcpyAsync(scratch + o, f.first, f.second * sizeof(T), cudaMemcpyDeviceToDevice, stream);
+        o += f.second;
       }
     }
-    set_tile(br, bc);
-    if (rr) *rr = br;
-    if (cc) *cc = bc;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    std::vector<int> h_uv(kSlots);
+    std::vector<long long> h_steps(kSlots), h_nan(kSlots);
+    std::vector<double> h_beta(kSlots), h_diag(3 * kSlots);
+    if (e == cudaSuccess) e = cudaMemcpy(h_uv.data(), d_uvslot, sizeof(int) * kSlots, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(h_steps.data(), d_steps, sizeof(long long) * kSlots, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(h_nan.data(), d_nan, sizeof(long long) * kSlots, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(h_beta.data(), d_beta, sizeof(double) * kSlots, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(h_diag.data(), d_diag, sizeof(double) * 3 * kSlots, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+      cudaFree(scratch);
+      return fail(GDC_E_CUDA, cuda_msg("autotune: save", e));
+    }
+    const std::vector<MemberRec> saved_recs = recs;
+    const int saved_old = old_, saved_new = new_;
+    std::array<int, 4> pick = {tile_r, tile_c, split_mode, fuse_final ? 1 : 0};
+    // No member may finish while the candidates are timed.
+    for (int sl : active_slots) recs[sl].nsteps = recs[sl].steps_done + (1LL << 40);
+
+    // --- time the candidates
+    std::vector<std::array<int, 4>> cand;  // rows, cols, split, fuse
+    const int shapes[][2] = {{16, 64}, {8, 64}, {8, 32}, {4, 128}, {4, 32}, {16, 30}};
+    for (auto& sh : shapes) {
+      const bool st = strip_shape_supported(sh[0], sh[1]);
+      if (!st && !tile_shape_supported(sh[0], sh[1], sizeof(T) == 8)) continue;
+      for (int split = 0; split <= 1; ++split)
+        for (int fuse = 0; fuse <= (st ? 0 : 1); ++fuse) cand.push_back({sh[0], sh[1], split, fuse});
+    }
+    const int reps = 3;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    double best = 1e30;
+    int rc = GDC_OK;
+    for (auto& c : cand) {
+      rc = set_tile(c[0], c[1]);
+      if (rc == GDC_OK) rc = set_schedule(c[2], c[3]);
+      if (rc == GDC_OK) rc = step(2);  // build, capture both time-level parities
+      std::vector<float> t;
+      for (int k = 0; k < reps && rc == GDC_OK; ++k) {
+        cudaEventRecord(e0, stream);
+        rc = step(1);
+        cudaEventRecord(e1, stream);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        t.push_back(ms);
+      }
+      if (rc) break;
+      std::sort(t.begin(), t.end());
+      if (t[reps / 2] < best) {
+        best = t[reps / 2];
+        pick = c;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+
+    // --- restore
+    sync_stream();
+    e = cudaSuccess;
+    for (auto& sv : saves) {
+      size_t o = sv.off;
+      const MemberDev<T>& d = hdesc[sv.slot];
+      const int lvl = saved_recs[sv.slot].level;
+      // the level's fields go back to the slot that held them
+      std::vector<T*> dst;
+      for (int f = 0; f < 3; ++f) {
+        dst.push_back(d.st[lvl][f]);
+        if (d.lo[lvl][f]) dst.push_back(d.lo[lvl][f]);
+      }
+      dst.push_back(d.given_u);
+      dst.push_back(d.given_v);
+      for (size_t q = 0; q < sv.fields.size(); ++q) {
+        if (e == cudaSuccess)
+          e = cudaMemcpyAsync(dst[q], scratch + o, sv.fields[q].second * sizeof(T), cudaMemcpyDeviceToDevice, stream);
+        o += sv.fields[q].second;
+      }
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e == cudaSuccess) e = cudaMemcpy(d_uvslot, h_uv.data(), sizeof(int) * kSlots, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_steps, h_steps.data(), sizeof(long long) * kSlots, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_nan, h_nan.data(), sizeof(long long) * kSlots, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_beta, h_beta.data(), sizeof(double) * kSlots, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_diag, h_diag.data(), sizeof(double) * 3 * kSlots, cudaMemcpyHostToDevice);
+    cudaFree(scratch);
+    recs = saved_recs;
+    old_ = saved_old;
+    new_ = saved_new;
+    set_tile(pick[0], pick[1]);
+    set_schedule(pick[2], pick[3]);
+    invalidate_graphs();
+    dirty = true;
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("autotune: restore", e));
+    if (rr) *rr = pick[0];
+    if (cc) *cc = pick[1];
     if (best_ms) *best_ms = best;
+    return GDC_OK;
+  }
+
+  int get_schedule(int* r, int* c, int* split, int* fuse) override {
+    if (r) *r = tile_r;
+    if (c) *c = tile_c;
+    if (split) *split = split_mode;
+    if (fuse) *fuse = fuse_final ? 1 : 0;
     return GDC_OK;
   }
 
@@ -1046,7 +1172,10 @@ class Batch final : public BatchIface {
   // critical path); otherwise one task per row stages the row once.
   bool split_rows = sizeof(T) == 8;
   int split_mode = -1;     // -1 automatic (above), 0 whole rows, 1 split by field
-  bool fuse_final = true;  // predict_correct's update formed in the next one's first stage
+  // predict_correct's update formed in the next one's first stage: correct
+  // and tested, but measured slower (the first stage is latency-bound and
+  // the update's loads land on its critical path), so off by default.
+  bool fuse_final = false;
   int num_sms = 152;
   // With strips, the whole-row tasks run on a second stream, concurrently
   // with the strips over the ordinary rows.
@@ -1063,10 +1192,11 @@ class Batch final : public BatchIface {
   std::vector<Prof> prof;
   std::vector<void*> allocs;
 
-  // Fastest measured: FP32 16x64 tiles on the 64-member ensemble, FP64
-  // 8x32 on the single 360x181 member.
-  int default_rows() const { return weno() ? 8 : (sizeof(T) == 4 ? 16 : 8); }
-  int default_cols() const { return weno() ? 32 : (sizeof(T) == 4 ? 64 : 32); }
+  // Fastest measured: 16x64 tiles, in FP32 on the 64-member ensemble and in
+  // FP64 on the single 360x181 member (one tile per SM: each tile has an
+  // SM's FP64 pipe to itself).
+  int default_rows() const { return weno() ? 8 : 16; }
+  int default_cols() const { return weno() ? 32 : 64; }
   bool weno() const { return P.uv_adv_scheme == GDC_ADV_WENO; }
 
   // The diffusion and copy kernels run on 8x32, 8x64 or 4x128 tiles.
@@ -1774,6 +1904,9 @@ int gdc_batch_active(gdc_batch* b, int* n) { return (b && n) ? b->impl->active(n
 int gdc_batch_set_tile(gdc_batch* b, int r, int c) { return b ? b->impl->set_tile(r, c) : GDC_E_CONFIG; }
 int gdc_batch_set_schedule(gdc_batch* b, int split_rows, int fuse_final) {
   return b ? b->impl->set_schedule(split_rows, fuse_final) : GDC_E_CONFIG;
+}
+int gdc_batch_get_schedule(gdc_batch* b, int* tile_rows, int* tile_cols, int* split_rows, int* fuse_final) {
+  return b ? b->impl->get_schedule(tile_rows, tile_cols, split_rows, fuse_final) : GDC_E_CONFIG;
 }
 int gdc_batch_history(gdc_batch* b, int member_id, double* u_a, double* v_a, double* gh, double* div, double* vor,
                       int ld) {

@@ -301,8 +301,11 @@ struct DiagArgs {
 
 // Tile shapes compiled for the stage and diffusion kernels (rows x columns),
 // and the warp-strip layouts of the stage kernel (band rows x kStripCols).
-inline bool tile_shape_supported(int r, int c) {
-  return (r == 8 && c == 32) || (r == 8 && c == 64) || (r == 4 && c == 128) || (r == 16 && c == 64);
+// 4x32 (fewer points than threads: finer load balance where FP64 work per
+// point is large) is compiled for FP64 only.
+inline bool tile_shape_supported(int r, int c, bool fp64) {
+  return (r == 8 && c == 32) || (r == 8 && c == 64) || (r == 4 && c == 128) || (r == 16 && c == 64) ||
+         (fp64 && r == 4 && c == 32);
 }
 inline bool strip_shape_supported(int r, int c) { return c == kStripCols && (r == 8 || r == 16 || r == 32 || r == 64); }
 

@@ -159,6 +159,18 @@ __device__ inline V block_value(A a, V* red) {
   return block_acc(a, red).value();
 }
 
+// The 16-byte vector of a compute type.
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+  using type = float4;
+};
+template <>
+struct Vec16<double> {
+  using type = double2;
+};
+
 // 4- or 8-byte asynchronous global->shared copy; src-size 0 zero-fills.
 template <typename T>
 __device__ __forceinline__ void cp_async(T* smem, const T* gmem, bool valid) {
@@ -324,49 +336,80 @@ __device__ void tile_issue(const MemberDev<T>& md, const T* __restrict__ gd, con
 // as final_kernel forms it -- and the block writes the level (and its
 // compensation words) for the points it owns: rows 1..vrows, columns
 // 1..vcols of the tile, of the fields in `own_fields` (bit f for field f).
+// Row interiors go 16 bytes at a time (shared, compensation words and the
+// level's stores), the three halo columns element by element.
+template <typename T>
+__device__ __forceinline__ T combine_level(T x, const T* lo, T tv, T h, T* e) {
+  if (lo) {
+    const T y = *lo + h * tv;
+    const T sum = x + y;
+    const T bp = sum - x;
+    *e = (x - (sum - bp)) + (y - bp);
+    return sum;
+  }
+  return x + h * tv;
+}
+
 template <typename T, int R, int W>
 __device__ void tile_combine(const MemberDev<T>& md, const StageArgs& a, int member, Tile<T, R, W>& t,
                              int own_fields) {
   using TL = Tile<T, R, W>;
+  using V = typename Vec16<T>::type;
+  constexpr int VEC = TL::VEC, NCH = W / VEC;
   const int N = md.N, M = md.M, Mh = md.Mh;
   const T h = T(md.pcdt[a.fin_pass] * a.fin_h_scale * a.beta[member]);
   T* const* lo = md.lo[a.fin_base];
   T* const* out = md.st[a.in_slot];
   T* const* olo = md.lo[a.in_slot];
-  constexpr int CW = W + 3;  // staged columns i0-1 .. i0+W+1
+  T* hi[3] = {t.gd, t.iu, t.iv};
+  const T* tt[3] = {t.ig, t.u, t.v};
   cp_async_wait_all();
   __syncthreads();
-  for (int q = threadIdx.x; q < TL::ROWS * CW; q += kThreads) {
-    const int rr = q / CW, cc = q - rr * CW;
-    if (rr > t.vrows + 2 || cc > t.vcols + 2) continue;  // not staged
+  // row interiors (columns i0 .. i0+vcols-1, never wrapping, 16-byte aligned)
+  for (int q = threadIdx.x; q < TL::ROWS * NCH; q += kThreads) {
+    const int rr = q / NCH, k = q - rr * NCH;
+    if (rr > t.vrows + 2 || k * VEC >= t.vcols) continue;  // not staged
     const int j = t.j0 - 1 + rr;
     if (j < 0 || j >= M) continue;  // off the sphere: zero, as staged
-    int i = t.i0 - 1 + cc;
-    i = i < 0 ? i + N : (i >= N ? i - N : i);
-    const int p = TL::pos(rr, cc);
-    const bool own = rr >= 1 && rr <= t.vrows && cc >= 1 && cc <= t.vcols;
-    const size_t o = (size_t)j * N + i;
-    T* hi[3] = {t.gd, t.iu, t.iv};
-    const T* tt[3] = {t.ig, t.u, t.v};
+    const int p = TL::pos(rr, 1 + k * VEC);
+    const size_t o = (size_t)j * N + t.i0 + k * VEC;
+    const bool own = rr >= 1 && rr <= t.vrows;
 #pragma unroll
     for (int f = 0; f < 3; ++f) {
       if (f == F_IV && j >= Mh) continue;
-      const T x = hi[f][p];
-      if (lo[f]) {
-        const T y = lo[f][o] + h * tt[f][p];
-        const T sum = x + y;
-        const T bp = sum - x;
-        const T e = (x - (sum - bp)) + (y - bp);
-        hi[f][p] = sum;
-        if (own && (own_fields >> f & 1)) {
-          out[f][o] = sum;
-          olo[f][o] = e;
-        }
-      } else {
-        const T sum = x + h * tt[f][p];
-        hi[f][p] = sum;
-        if (own && (own_fields >> f & 1)) out[f][o] = sum;
+      V x = *reinterpret_cast<const V*>(hi[f] + p);
+      const V tv = *reinterpret_cast<const V*>(tt[f] + p);
+      V l, e;
+      if (lo[f]) l = *reinterpret_cast<const V*>(lo[f] + o);
+      T* xs = reinterpret_cast<T*>(&x);
+      const T* ts = reinterpret_cast<const T*>(&tv);
+      const T* ls = reinterpret_cast<const T*>(&l);
+      T* es = reinterpret_cast<T*>(&e);
+#pragma unroll
+      for (int m = 0; m < VEC; ++m) xs[m] = combine_level(xs[m], lo[f] ? ls + m : nullptr, ts[m], h, es + m);
+      *reinterpret_cast<V*>(hi[f] + p) = x;
+      if (own && (own_fields >> f & 1)) {
+        *reinterpret_cast<V*>(out[f] + o) = x;
+        if (lo[f]) *reinterpret_cast<V*>(olo[f] + o) = e;
       }
+    }
+  }
+  // halo columns i0-1, i0+vcols, i0+vcols+1 (periodic): never owned
+  for (int q = threadIdx.x; q < TL::ROWS * 3; q += kThreads) {
+    const int rr = q / 3, hh = q - rr * 3;
+    if (rr > t.vrows + 2) continue;
+    const int j = t.j0 - 1 + rr;
+    if (j < 0 || j >= M) continue;
+    const int cc = hh == 0 ? 0 : t.vcols + hh;
+    int i = t.i0 - 1 + cc;
+    i = i < 0 ? i + N : (i >= N ? i - N : i);
+    const int p = TL::pos(rr, cc);
+    const size_t o = (size_t)j * N + i;
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      if (f == F_IV && j >= Mh) continue;
+      T e;
+      hi[f][p] = combine_level(hi[f][p], lo[f] ? lo[f] + o : nullptr, tt[f][p], h, &e);
     }
   }
   __syncthreads();
@@ -377,7 +420,7 @@ __device__ void tile_combine(const MemberDev<T>& md, const StageArgs& a, int mem
 // j0-1..j0+R (local 0..R+1), columns i0-1..i0+W (local 0..W+1).
 template <typename T, int R, int W>
 __device__ void tile_derive(const MemberDev<T>& md, Tile<T, R, W>& t, bool u_halo_row = false,
-                            bool given = false, bool want_v = true) {
+                            bool given = false, bool want_v = true, bool want_u = true) {
   using TL = Tile<T, R, W>;
   const int M = md.M, Mh = md.Mh;
   const int urow0 = u_halo_row ? 0 : 1;
@@ -396,7 +439,7 @@ __device__ void tile_derive(const MemberDev<T>& md, Tile<T, R, W>& t, bool u_hal
       t.ig[p] = g0;
       if (given) continue;
       T uu = 0, vv = 0;
-      if (rr >= urow0 && j >= 1 && j <= M - 2) uu = t.iu[p] * T(2) / (g0 + sqrt(t.gd[p + 1]));
+      if (want_u && rr >= urow0 && j >= 1 && j <= M - 2) uu = t.iu[p] * T(2) / (g0 + sqrt(t.gd[p + 1]));
       if (want_v && j >= 0 && j < Mh) vv = t.iv[p] * T(2) / (g0 + sqrt(t.gd[p + TL::SW]));
       t.u[p] = uu;
       t.v[p] = vv;
@@ -413,7 +456,7 @@ __device__ void tile_derive(const MemberDev<T>& md, Tile<T, R, W>& t, bool u_hal
     const int j = t.j0 - 1 + rr;
     const bool need = rr <= t.vrows + 1 && cc <= t.vcols + 1;
     T uu = 0, vv = 0;
-    if (need && rr >= urow0 && j >= 1 && j <= M - 2) uu = t.iu[p] * T(2) / (t.ig[p] + t.ig[p + 1]);
+    if (want_u && need && rr >= urow0 && j >= 1 && j <= M - 2) uu = t.iu[p] * T(2) / (t.ig[p] + t.ig[p + 1]);
     if (want_v && need && j >= 0 && j < Mh) vv = t.iv[p] * T(2) / (t.ig[p] + t.ig[p + TL::SW]);
     t.u[p] = uu;
     t.v[p] = vv;
@@ -904,8 +947,11 @@ __device__ __forceinline__ void bulk_tile(const MemberDev<T>& md, const StageArg
                                           T* staging, bool given, const T* gd_in, const T* iu_in,
                                           const T* iv_in, T ub_lon, T ub_lat, Emit<T>& em) {
   using TL = Tile<T, R, W>;
-  constexpr int RPT = R * W / kThreads;
-  static_assert(RPT * kThreads == R * W, "a tile is a whole number of rows per thread");
+  // Rows per thread; a tile with fewer points than threads leaves the
+  // threads past R*W without points (they stage and derive only).
+  constexpr int RPT = R * W >= kThreads ? R * W / kThreads : 1;
+  static_assert(R * W < kThreads ? kThreads % W == 0 : RPT * kThreads == R * W,
+                "a tile is a whole number of rows per thread");
   const int N = md.N;
   TL t = carve<T, R, W>(staging, w.j0, w.i0, w.rows, w.cols);
   const bool fuse = UF == UF_PREDICT_IN && a.fuse;
@@ -1553,7 +1599,8 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
       __syncthreads();
       tile_issue(md, gd_in, iu_in, iv_in, t, given, PASS != kSlowPass, fuse ? md.td[TS_NEW] : nullptr);
       if (fuse) tile_combine(md, a, w.member, t, f < 0 ? 7 : (1 << f));
-      tile_derive(md, t, false, given, PASS != kFastPass);
+      // A gd-only task (mass divergence, pole cap) reads no u and no v.
+      tile_derive(md, t, false, given, PASS != kFastPass && f != F_GD, f != F_GD);
       for (int c = threadIdx.x; c < vw; c += blockDim.x) {
         const int p = TR::pos(1, c + 1);
         const int i = c0 + c;
@@ -1679,16 +1726,6 @@ __global__ void __launch_bounds__(kThreads)
 // (src/dycore_mod.F90:789-790) over every point of the member.  FP32 time
 // levels carry a compensation word: new = (hi + lo) + dt*T via TwoSum.
 
-template <typename T>
-struct Vec16;
-template <>
-struct Vec16<float> {
-  using type = float4;
-};
-template <>
-struct Vec16<double> {
-  using type = double2;
-};
 
 // One flat item: a contiguous run of one field, 16 bytes per access.  All
 // of a thread's loads are issued before its first store.
@@ -2239,6 +2276,7 @@ size_t stage_smem_bytes(int tile_rows, int tile_cols, int max_n, int* staging_wo
   if (tile_rows == 8 && tile_cols == 64) bulk = tile_words<T, 8, 64>();
   if (tile_rows == 16 && tile_cols == 64) bulk = tile_words<T, 16, 64>();
   if (tile_rows == 4 && tile_cols == 128) bulk = tile_words<T, 4, 128>();
+  if (tile_rows == 4 && tile_cols == 32) bulk = tile_words<T, 4, 32>();
   // A block is a bulk tile or a whole-row task: the row task's tile, rows,
   // kept coefficients and twiddles share the bulk tile's staging area.
   // Rounded to 4 words and max_n to an even count so that the FP64
@@ -2306,6 +2344,8 @@ int launch_stage(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int adv
   if (tile_rows == 8 && tile_cols == 64) return launch_stage_shape<T, 8, 64>(mem, wl, nwork, adv, max_n, a, s);
   if (tile_rows == 16 && tile_cols == 64) return launch_stage_shape<T, 16, 64>(mem, wl, nwork, adv, max_n, a, s);
   if (tile_rows == 4 && tile_cols == 128) return launch_stage_shape<T, 4, 128>(mem, wl, nwork, adv, max_n, a, s);
+  if constexpr (sizeof(T) == 8)
+    if (tile_rows == 4 && tile_cols == 32) return launch_stage_shape<T, 4, 32>(mem, wl, nwork, adv, max_n, a, s);
   return GDC_E_CONFIG;
 }
 

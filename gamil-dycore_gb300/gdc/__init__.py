@@ -154,6 +154,7 @@ def lib() -> ctypes.CDLL:
             "gdc_batch_active": (ctypes.c_int, [vp, ip]),
             "gdc_batch_set_tile": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
             "gdc_batch_set_schedule": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
+            "gdc_batch_get_schedule": (ctypes.c_int, [vp, ip, ip, ip, ip]),
             "gdc_batch_checkpoint": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_char_p]),
             "gdc_batch_restore": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_size_t, ip]),
             "gdc_write_restart": (ctypes.c_int, [vp, ctypes.c_char_p]),
@@ -505,9 +506,18 @@ class Batch:
         self._check(lib().gdc_batch_set_schedule(self.b, split_rows, fuse_final))
 
     def autotune(self):
+        """Time every launch schedule on the current members and keep the
+        fastest; the members' states are restored.  Returns (tile rows, tile
+        columns, ms per model step)."""
         r, c, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
         self._check(lib().gdc_batch_autotune(self.b, ctypes.byref(r), ctypes.byref(c), ctypes.byref(ms)))
         return r.value, c.value, ms.value
+
+    def schedule(self) -> dict:
+        """The launch schedule in use: tile shape, row-task split, fusion."""
+        v = [ctypes.c_int() for _ in range(4)]
+        self._check(lib().gdc_batch_get_schedule(self.b, *[ctypes.byref(x) for x in v]))
+        return {"tile": (v[0].value, v[1].value), "split_rows": v[2].value, "fuse_final": v[3].value}
 
     def profile(self, nsteps: int):
         ms = (ctypes.c_double * 5)()

@@ -313,11 +313,15 @@ int gdc_batch_diag(gdc_batch* b, int member_id, double* total_mass,
 int gdc_batch_active(gdc_batch* b, int* n_active);
 
 /* Work layout of the stage kernels: shared-memory tiles of rows x columns
- * (8x32, 8x64, 4x128, 16x64) or warp strips of rows x 30 columns (8x30, 16x30,
- * 32x30, 64x30: one warp marches a 30-column strip down a band of rows);
- * 0,0 picks the default (FP32 16x64, FP64 8x32 tiles).
- * gdc_batch_autotune times the candidates on the current members and keeps
- * the fastest; the chosen shape is returned. */
+ * (8x32, 8x64, 4x128, 16x64; 4x32 in FP64) or warp strips of rows x 30
+ * columns (8x30, 16x30, 32x30, 64x30: one warp marches a 30-column strip
+ * down a band of rows); 0,0 picks the default (16x64 tiles; 8x32 for
+ * WENO).  gdc_batch_autotune times every supported shape under each
+ * schedule of gdc_batch_set_schedule on the current members and keeps the
+ * fastest; the members' states and step counts are saved before and
+ * restored after, so tuning advances no forecast.  It returns the chosen
+ * shape and its time per model step; gdc_batch_get_schedule reports the
+ * whole choice. */
 int gdc_batch_set_tile(gdc_batch* b, int tile_rows, int tile_cols);
 /* Launch schedule of the stage kernels (a choice of how the work is
  * split, which gdc_batch_autotune also tunes): split_rows -1 picks
@@ -327,10 +331,11 @@ int gdc_batch_set_tile(gdc_batch* b, int tile_rows, int tile_cols);
  * forms each predict_correct's final update (src/dycore_mod.F90:789-790)
  * in the first stage of the next predict_correct of the same step instead
  * of a launch of its own (tiles only; WENO batches and warp strips always
- * launch it).  FP64 results are bitwise the same under every schedule;
+ * launch it), 0 (default) launches it.  FP64 results are bitwise the same under every schedule;
  * FP32 results agree to rounding (the partial sums of beta group
  * differently). */
 int gdc_batch_set_schedule(gdc_batch* b, int split_rows, int fuse_final);
+int gdc_batch_get_schedule(gdc_batch* b, int* tile_rows, int* tile_cols, int* split_rows, int* fuse_final);
 int gdc_batch_autotune(gdc_batch* b, int* tile_rows, int* tile_cols,
                        double* best_ms_per_step);
 

@@ -65,10 +65,11 @@ def test_fp32_compensated_vs_fp64(native):
     assert e[2] <= 1e-5, e
 
 
-@pytest.mark.parametrize("tile", [(8, 32), (8, 64), (4, 128), (16, 64)])
+@pytest.mark.parametrize("tile", [(8, 32), (8, 64), (4, 128), (16, 64), (4, 32)])
 def test_every_tile_shape_matches_oracle_on_ragged_grid(native, tile):
     """720 columns leave a ragged last column block under every tile shape
-    (16, 16 and 80 columns), whose halo columns wrap to 0 and 1."""
+    (16, 16 and 80 columns), whose halo columns wrap to 0 and 1; 4x32 tiles
+    have fewer points than the block has threads."""
     from oracle.oracle import OracleModel
     N, M = 720, 361
     p = scheme(gdc, N, M, 120.0, subcycles=2, cutoff=(4,) * 5)
@@ -162,3 +163,80 @@ def test_warp_strips_other_schemes_match_oracle(native, split, adv):
     ref = o.get_state()
     for name, a in zip(("u", "v", "gd"), got):
         assert np.array_equal(interior(a), interior(ref[name])), (split, adv, name)
+
+
+@pytest.mark.parametrize("split", [0, 1])
+def test_every_schedule_matches_oracle(native, split):
+    """Whole-row or per-field row tasks, the final update launched or formed
+    by the next predict_correct's first stage: the FP64 path stays bitwise
+    the oracle's (csp2 with 6 subcycles: seven fused updates per step)."""
+    from oracle.oracle import OracleModel
+    N, M = 360, 181
+    p = scheme(gdc, N, M, 240.0)
+    ic = gdc.ic_seeded(N, M, seed=6)
+    o = OracleModel.from_params(p)
+    o.set_state(*ic)
+    o.step(3)
+    ref = o.get_state()
+    for fuse in (0, 1):
+        b = gdc.Batch(p)
+        b.set_schedule(split, fuse)
+        mid = b.add(N, M, 240.0, 3, *ic)
+        b.step(3)
+        b.sync()
+        assert b.schedule()["fuse_final"] == fuse
+        for name, a in zip(("u", "v", "gd"), b.get_state(mid)):
+            assert np.array_equal(interior(a), interior(ref[name])), (split, fuse, name)
+        b.close()
+
+
+def test_fp32_fused_schedule_matches_launched(native):
+    """FP32 under the fused schedule: the update's arithmetic is
+    final_kernel's, so the state is bitwise the launched schedule's."""
+    N, M = 180, 91
+    p = scheme(gdc, N, M, 480.0, precision=gdc.FP32)
+    ic = gdc.ic_seeded(N, M, seed=3)
+    out = []
+    for fuse in (0, 1):
+        b = gdc.Batch(p)
+        b.set_schedule(-1, fuse)
+        mid = b.add(N, M, 480.0, 10, *ic)
+        b.step(10)
+        out.append(b.get_state(mid))
+        b.close()
+    for x, y in zip(*out):
+        assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("prec", [gdc.FP64, gdc.FP32])
+def test_autotune_advances_no_forecast(native, prec):
+    """Autotuning times every schedule on the live members and restores
+    them: the state right after is the state before, and the run continues
+    exactly as in an untuned twin batch (bitwise in FP64 under any chosen
+    schedule; in FP32 the twin uses the same schedule)."""
+    p = scheme(gdc, 360, 181, 240.0, precision=prec)
+    ics = [gdc.ic_seeded(360, 181, seed=1), gdc.ic_seeded(180, 91, seed=2)]
+    grids = [(360, 181, 240.0), (180, 91, 480.0)]
+    a, b = gdc.Batch(p), gdc.Batch(p)
+    ia = [a.add(N, M, dt, 9, *ic) for (N, M, dt), ic in zip(grids, ics)]
+    ib = [b.add(N, M, dt, 9, *ic) for (N, M, dt), ic in zip(grids, ics)]
+    a.step(2)
+    b.step(2)
+    before = [a.get_state(i) for i in ia]
+    diag_before = [a.diag(i) for i in ia]
+    r, c, ms = a.autotune()
+    assert ms > 0 and (r, c) == a.schedule()["tile"]
+    for i, s0, d0 in zip(ia, before, diag_before):
+        for x, y in zip(s0, a.get_state(i)):
+            assert np.array_equal(x, y)
+        assert a.diag(i) == d0 and a.info(i)[0] == 2
+    sch = a.schedule()
+    if prec == gdc.FP32:
+        b.set_tile(*sch["tile"])
+        b.set_schedule(sch["split_rows"], sch["fuse_final"])
+    a.step(7)
+    b.step(7)
+    for i, j in zip(ia, ib):
+        assert a.info(i)[:2] == (9, 1)
+        for x, y in zip(a.get_state(i), b.get_state(j)):
+            assert np.array_equal(x, y)
