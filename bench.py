@@ -13,7 +13,7 @@ steps per second over the timed steps with the inputs resident in HBM; the
 plain FP64 path (360x181, 360 steps) is timed beside it.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload batch|plain|large-run]
+                  [--workload batch|plain|serve|large-run] [--requests N]
 
 --impl reference times the reference's arithmetic on the host cores: the
 oracle's reference-order restatement (the Fortran reference cannot be built
@@ -376,38 +376,74 @@ def beside_path(gdc, torch):
 
 def serve_sample(gdc, ts, n=40, rate=20.0, seed=0):
     """The serving loop on the first `n` requests of the Poisson stream
-    (20 requests/s; grids 180x91..1440x721; 6 h to 5 days), FP32."""
+    (20 requests/s; grids 180x91..1440x721; 6 h to 5 days), FP32; one batch
+    per subcycle class, each on its own stream."""
     from gdc import serve
     reqs = serve.poisson_stream(n=2000, rate=rate, seed=seed)[:n]
-    srv = serve.Server(precision=gdc.FP32, steps_per_tick=4, cuda_stream=ts.cuda_stream)
+    srv = serve.Server(precision=gdc.FP32, steps_per_tick=4)
     st = srv.run(reqs)
     srv.close()
     st.update({"max_resident": srv.max_resident, "ticks": srv.ticks, "steps_per_tick": 4,
+               "subcycles": dict((str(g), m) for g, m in serve.SUBCYCLES.items()),
                "sample": f"first {n} of 2000 requests of the Poisson stream (rate {rate}/s, seed {seed}); "
                          f"offered load exceeds one GPU's rate, so latency includes queueing"})
     return st
 
 
+def serve_run(args):
+    """The serving configuration: a Poisson stream of --requests requests at
+    20 per second (grid uniform over 180x91..1440x721, length uniform in
+    6 h..5 days, dt 240 s per degree), admitted by free device memory into
+    continuously batched FP32 steps; p50/p99 time to completion and the
+    aggregate grid-point steps per second."""
+    import __graft_entry__
+    __graft_entry__.build()
+    import gdc
+    from gdc import serve
+    reqs = serve.poisson_stream(n=args.requests, rate=20.0, seed=0)
+    srv = serve.Server(precision=gdc.FP32, steps_per_tick=4)
+    t0 = time.perf_counter()
+    st = srv.run(reqs)
+    wall = time.perf_counter() - t0
+    srv.close()
+    st.update({"workload": "serve", "wall_s": wall, "max_resident": srv.max_resident, "ticks": srv.ticks,
+               "steps_per_tick": 4, "subcycles": dict((str(g), m) for g, m in serve.SUBCYCLES.items()),
+               "stream": f"{args.requests} requests, Poisson 20/s, seed 0", "dtype": "f32"})
+    print(json.dumps(st), flush=True)
+
+
+def _rl2(a, b):
+    x, y = a[2:-2, 2:-2], b[2:-2, 2:-2]
+    return float((((x - y) ** 2).sum() / (y * y).sum()) ** 0.5)
+
+
 def large_run(args):
-    """1440x721, dt 60 s, FP32 (compensated levels; FP64 pole caps and
-    integrals) for args.days model days, and the FP64 path (bitwise equal to
-    the oracle) for args.fp64_days: mass and total-energy drift per day,
-    relative L2 of gd, u, v FP32 vs FP64 at the last FP64 day.  Initial
-    state: degree 1..12 seeded harmonics plus 3 seeded 2000 m mountains."""
+    """1440x721, dt 60 s, 8 subcycles: FP32 (compensated levels; FP64 pole
+    caps and integrals) for args.days model days and the FP64 path (bitwise
+    equal to the oracle) for args.fp64_days, with mass and total-energy
+    drift per day; for each FP64 day the relative L2 of gd, u, v FP32 vs
+    FP64, beside a perturbation-growth control: the FP64 run started from
+    its state with gd perturbed by 1e-13 relative (seeded), vs the FP64
+    run.  Initial state: degree 1..12 seeded harmonics plus 3 seeded 2000 m
+    mountains."""
     import numpy as np
     import __graft_entry__
     __graft_entry__.build()
     import gdc
     N, M, dt, spd, cut = GRIDS[1440]
     ic = gdc.ic_seeded(N, M, seed=0, lmax=12, n_mountains=3, mountain_height=2000.0, mountain_radius_deg=20.0)
+    gd_p = ic[2].copy()
+    gd_p[2:-2, 2:-2] *= 1.0 + 1e-13 * np.random.default_rng(0).uniform(-1.0, 1.0, size=gd_p[2:-2, 2:-2].shape)
+    ic_p = (ic[0], ic[1], gd_p, ic[3])
     out = {"workload": "large-run", "grid": f"{N}x{M}", "dt": dt, "subcycles": 8, "days": args.days,
-           "fp64_days": args.fp64_days}
+           "fp64_days": args.fp64_days, "perturbation": "gd x (1 + 1e-13 U(-1,1)), seed 0"}
     states = {}
-    for prec, days in ((gdc.FP32, args.days), (gdc.FP64, args.fp64_days)):
+    for key, prec, days, start in (("fp32", gdc.FP32, args.days, ic), ("fp64", gdc.FP64, args.fp64_days, ic),
+                                   ("fp64_perturbed", gdc.FP64, args.fp64_days, ic_p)):
         p = gdc.default_params(num_lon=N, num_lat=M, time_step_size=dt, subcycles=8, split_scheme=gdc.SPLIT_CSP2,
                                qcon_modified=1, zonal_tend_filter_cutoff_wavenumber=cut, precision=prec)
         b = gdc.Batch(p)
-        mid = b.add(N, M, dt, days * spd, *ic)
+        mid = b.add(N, M, dt, days * spd, *start)
         m0, e0, _ = b.diag(mid)
         rows = []
         t = time.perf_counter()
@@ -417,19 +453,56 @@ def large_run(args):
             m, e, beta = b.diag(mid)
             rows.append({"day": d, "mass_drift": (m - m0) / m0, "energy_drift": (e - e0) / e0, "beta": beta,
                          "nan_step": b.info(mid)[2]})
+            if d <= args.fp64_days:
+                states[(key, d)] = b.get_state(mid)
         secs = time.perf_counter() - t
-        states[prec] = b.get_state(mid)
         b.close()
-        key = "fp32" if prec == gdc.FP32 else "fp64"
         out[key] = {"per_day": rows, "seconds": secs, "grid_pt_steps_per_s": N * M * days * spd / secs}
-
-    def rl2(a, b):
-        x, y = a[2:-2, 2:-2], b[2:-2, 2:-2]
-        return float(np.sqrt(np.sum((x - y) ** 2) / np.sum(y * y)))
-    s32, s64 = states[gdc.FP32], states[gdc.FP64]
-    if args.days == args.fp64_days:
-        out["l2_fp32_vs_fp64"] = {"gd": rl2(s32[2], s64[2]), "u": rl2(s32[0], s64[0]), "v": rl2(s32[1], s64[1])}
+    out["l2_vs_fp64"] = []
+    for d in range(1, min(args.days, args.fp64_days) + 1):
+        ref = states[("fp64", d)]
+        row = {"day": d}
+        for key in ("fp32", "fp64_perturbed"):
+            s_ = states[(key, d)]
+            row[key] = {"gd": _rl2(s_[2], ref[2]), "u": _rl2(s_[0], ref[0]), "v": _rl2(s_[1], ref[1])}
+        out["l2_vs_fp64"].append(row)
     print(json.dumps(out), flush=True)
+
+
+def precision_config1(gdc, torch, ts, rtol=1e-5):
+    """The precision configuration: 720x361, dt 120 s, 720 steps (one model
+    day), a uniform zonal flow u = 20 cos(lat) m/s in geostrophic balance
+    over 3 seeded 2000 m Gaussian mountains (20 degree e-folding radius),
+    gd0 = 5960 m g; FP32 with compensated time levels against the FP64 path.
+    The zonal flow makes the reference's filter rescale noise-driven on the
+    filtered rows, so both runs use the rescale guard (rtol)."""
+    N, M, dt = 720, 361, 120.0
+    ic = gdc.ic_seeded(N, M, seed=1, lmax=0, gd0=5960 * G, gd_rms=0.0, psi_rms=0.0, u0=20.0, n_mountains=3,
+                       mountain_height=2000.0, mountain_radius_deg=20.0)
+    out, st = {}, {}
+    for name, prec in (("fp64", gdc.FP64), ("fp32", gdc.FP32)):
+        p = gdc.default_params(num_lon=N, num_lat=M, time_step_size=dt, subcycles=6, split_scheme=gdc.SPLIT_CSP2,
+                               qcon_modified=1, zonal_tend_filter_cutoff_wavenumber=[4] * 10, precision=prec,
+                               filter_rescale_rtol=rtol)
+        m = gdc.Model(p)
+        m.set_stream(ts.cuda_stream)
+        m.set_state(*ic)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(ts)
+        m.step(720)
+        e1.record(ts)
+        torch.cuda.synchronize()
+        m.sync()
+        out[name + "_grid_pt_steps_per_s"] = N * M * 720 / (e0.elapsed_time(e1) / 1e3)
+        st[name] = m.get_state()
+        m.close()
+    u32, v32, g32 = st["fp32"]
+    u64, v64, g64 = st["fp64"]
+    out["l2_fp32_vs_fp64"] = {"gd": _rl2(g32, g64), "u": _rl2(u32, u64), "v": _rl2(v32, v64)}
+    out["config"] = "720x361 dt 120 s, 720 steps, zonal flow over 3 mountains, csp2 6, cutoffs 4 x 10"
+    out["filter_rescale_rtol"] = rtol
+    return out
 
 
 def plain_run(args):
@@ -511,6 +584,7 @@ def run_ours(args, rank, world, dist):
     clocks = clk.summary()
     value, ms_all = replica_value(dist, gpt, ms)
     plain = plain_fp64(gdc, torch, ts)
+    precision = precision_config1(gdc, torch, ts)
     e2e_ms, e2e_gpt, h2d, d2h = e2e_batch(gdc, torch, members, args.steps, gdc.FP32, sched)
     e2e_ms = reduce_max(dist, e2e_ms)
     prof_ms, prof_n = profile_kernels(gdc, members, gdc.FP32, sched=sched)
@@ -568,6 +642,7 @@ def run_ours(args, rank, world, dist):
                        "fp32_single_member_value": plain["fp32_value"],
                        "l2_fp32_vs_fp64_after_1_day": plain["l2_fp32_vs_fp64"],
                        "batched_fp32_over_plain_fp64": value / plain["value"]},
+        "precision_720x361": precision,
         "serving": serving,
         "beside_path": beside,
         "nan_members": sum(1 for x in nan if x >= 0),
@@ -722,7 +797,8 @@ def main():
     ap.add_argument("--steps", type=int, default=720)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="batch", choices=["batch", "plain", "large-run"],
+    ap.add_argument("--requests", type=int, default=2000, help="serve: requests of the stream")
+    ap.add_argument("--workload", default="batch", choices=["batch", "plain", "serve", "large-run"],
                     help="plain: the FP64 path alone on the seeded 360x181 state; "
                          "large-run: 1440x721 FP32 for --days model days with per-day mass and energy drift, "
                          "beside the FP64 path for --fp64-days")
@@ -742,6 +818,8 @@ def main():
         large_run(args)
     elif args.workload == "plain":
         plain_run(args)
+    elif args.workload == "serve":
+        serve_run(args)
     else:
         run_ours(args, rank, world, dist)
     if dist is not None:

@@ -85,6 +85,37 @@ std::string cuda_msg(const char* what, cudaError_t e) {
   return std::string(what) + ": " + cudaGetErrorString(e);
 }
 
+// Host staging for uploads and read-backs: page-locked memory (copies run
+// at the host link's full rate and asynchronously), grown on demand; plain
+// host memory if page-locked memory cannot be had.
+struct PinnedStage {
+  char* p = nullptr;
+  size_t cap = 0;
+  bool pinned = false;
+  std::vector<char> fallback;
+  char* get(size_t n) {
+    if (n <= cap) return p;
+    if (pinned && p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    pinned = false;
+    const size_t want = std::max(n, (size_t)1 << 20);
+    if (cudaMallocHost((void**)&p, want) == cudaSuccess) {
+      pinned = true;
+      cap = want;
+      return p;
+    }
+    cudaGetLastError();
+    fallback.resize(n);
+    p = fallback.data();
+    cap = n;
+    return p;
+  }
+  ~PinnedStage() {
+    if (pinned && p) cudaFreeHost(p);
+  }
+};
+
 struct MemberRec {
   bool used = false, active = false, finished = false, nan = false;
   int N = 0, M = 0;
@@ -303,19 +334,30 @@ class Batch final : public BatchIface {
     d.given_u = (T*)(base + L.given_u);
     d.given_v = (T*)(base + L.given_v);
     for (int k = 0; k < 2; ++k) d.wadv[k] = L.wadv[k] == (size_t)-1 ? nullptr : (T*)(base + L.wadv[k]);
-    // Upload (synchronously: admission is a step-boundary operation).
-    sync_stream();
-    e = cudaMemset(r.dmem, 0, L.total);
-    if (e == cudaSuccess) e = cudaMemcpy(base + L.coef, coef.data(), coef.size() * sizeof(T), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(base + L.rowc, rowc.data(), rowc.size() * sizeof(T), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(base + L.twid, twid.data(), twid.size() * sizeof(T), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(base + L.rowinfo, r.rowinfo.data(), M * sizeof(int), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(base + L.dcoef, dco.data(), dco.size() * sizeof(double), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(d_mem + slot, &d, sizeof(d), cudaMemcpyHostToDevice);
-    const long long minus1 = -1, zero = 0;
-    if (e == cudaSuccess) e = cudaMemcpy(d_nan + slot, &minus1, sizeof(minus1), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(d_steps + slot, &zero, sizeof(zero), cudaMemcpyHostToDevice);
+    // Upload, on the stream from page-locked staging: the zeroed member, its
+    // tables (contiguous in the layout: one image, one copy), the descriptor
+    // and its step words.  The caller synchronises before it returns.
+    sync_stream();  // the staging areas may still feed an earlier copy
+    const size_t img = L.given_u - L.coef;
+    const size_t dsz = (sizeof(d) + 15) & ~size_t(15);
+    char* st = stage_tab.get(img + dsz + 2 * sizeof(long long));
+    std::memset(st, 0, img);
+    std::memcpy(st + (L.coef - L.coef), coef.data(), coef.size() * sizeof(T));
+    std::memcpy(st + (L.rowc - L.coef), rowc.data(), rowc.size() * sizeof(T));
+    std::memcpy(st + (L.twid - L.coef), twid.data(), twid.size() * sizeof(T));
+    std::memcpy(st + (L.rowinfo - L.coef), r.rowinfo.data(), M * sizeof(int));
+    std::memcpy(st + (L.dcoef - L.coef), dco.data(), dco.size() * sizeof(double));
+    std::memcpy(st + img, &d, sizeof(d));
+    long long* words = reinterpret_cast<long long*>(st + img + dsz);
+    words[0] = -1;  // nan step
+    words[1] = 0;   // steps done
+    e = cudaMemsetAsync(r.dmem, 0, L.total, stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(base + L.coef, st, img, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_mem + slot, st + img, sizeof(d), cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_nan + slot, words, sizeof(long long), cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_steps + slot, words + 1, sizeof(long long), cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess) {
+      sync_stream();
       release(slot);
       return fail(GDC_E_CUDA, cuda_msg("add: upload", e));
     }
@@ -367,8 +409,7 @@ class Batch final : public BatchIface {
     r.ic_ld = ld;
     r.ic_u.assign(u, u + (size_t)ld * (M + 4));
     r.ic_v.assign(v, v + (size_t)ld * (Mh + 4));
-    if (h_ic.size() < words) h_ic.resize(words);
-    double* hu = h_ic.data();
+    double* hu = reinterpret_cast<double*>(stage_ic.get(words * sizeof(double)));
     double* hv = hu + full;
     double* hg = hv + half;
     double* hh = hg + full;
@@ -765,13 +806,13 @@ class Batch final : public BatchIface {
     if (e == cudaSuccess) e = ensure_tmp(words);
     if (e == cudaSuccess && launch_state_out<T>(d_mem, id, lvl, uv_mode, N, M, d_ictmp, stream) != GDC_OK)
       e = cudaGetLastError();
-    if (h_ic.size() < words) h_ic.resize(words);
+    double* hbuf = reinterpret_cast<double*>(stage_ic.get(words * sizeof(double)));
     // gd, u, v first: the usual request copies only those
     const size_t back = (iu || iv || ig) ? words : 2 * n + nh;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(h_ic.data(), d_ictmp, back * sizeof(double), cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hbuf, d_ictmp, back * sizeof(double), cudaMemcpyDeviceToHost, stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("get_state", e));
-    const double* hg = h_ic.data();
+    const double* hg = hbuf;
     const double* ou = hg + n;
     const double* ov = ou + n;
     const double* hu = ov + nh;
@@ -1142,7 +1183,13 @@ class Batch final : public BatchIface {
   double* d_beta = nullptr;
   double* d_ictmp = nullptr;  // FP64 scratch: an admitted initial condition, a read-back level
   size_t ictmp_cap = 0;       // its capacity in doubles
-  std::vector<double> h_ic;   // host staging of the same
+  PinnedStage stage_ic;       // host staging of the same
+  PinnedStage stage_tab;      // host staging of an admitted member's tables
+  // the initial diagnostics' work items, partials and member slot
+  FlatItem* d_idl = nullptr;
+  double* d_ipart = nullptr;
+  int* d_islot = nullptr;
+  size_t idl_cap = 0;
   double* d_diag = nullptr;
   long long* d_steps = nullptr;
   long long* d_nan = nullptr;
@@ -1249,6 +1296,9 @@ class Batch final : public BatchIface {
     if (d_dpart) cudaFree(d_dpart);
     if (d_partials) cudaFree(d_partials);
     if (d_ictmp) cudaFree(d_ictmp);
+    if (d_idl) cudaFree(d_idl);
+    if (d_ipart) cudaFree(d_ipart);
+    if (d_islot) cudaFree(d_islot);
     if (own_stream) cudaStreamDestroy(own_stream);
     if (side) cudaStreamDestroy(side);
     if (ev_fork) cudaEventDestroy(ev_fork);
@@ -1714,33 +1764,46 @@ class Batch final : public BatchIface {
     std::vector<FlatItem> wl;
     const MemberDev<T> saved = hdesc[slot];
     append_diag_items(slot, wl);
-    FlatItem* dwl = nullptr;
-    double* dpart = nullptr;
-    int* dslot = nullptr;
-    if (cudaMalloc(&dwl, sizeof(FlatItem) * wl.size()) != cudaSuccess ||
-        cudaMalloc(&dpart, sizeof(double) * 4 * wl.size()) != cudaSuccess ||
-        cudaMalloc(&dslot, sizeof(int)) != cudaSuccess) {
+    if (wl.size() > idl_cap) {
+      if (d_idl) cudaFree(d_idl);
+      if (d_ipart) cudaFree(d_ipart);
+      d_idl = nullptr;
+      d_ipart = nullptr;
+      idl_cap = 0;
+      if (cudaMalloc(&d_idl, sizeof(FlatItem) * wl.size()) != cudaSuccess ||
+          cudaMalloc(&d_ipart, sizeof(double) * 4 * wl.size()) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(GDC_E_OOM, "initial diag: cudaMalloc");
+      }
+      idl_cap = wl.size();
+    }
+    if (!d_islot && cudaMalloc(&d_islot, sizeof(int)) != cudaSuccess) {
       cudaGetLastError();
-      if (dwl) cudaFree(dwl);
-      if (dpart) cudaFree(dpart);
       return fail(GDC_E_OOM, "initial diag: cudaMalloc");
     }
-    cudaError_t e = cudaMemcpy(dwl, wl.data(), sizeof(FlatItem) * wl.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(dslot, &slot, sizeof(int), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(d_mem + slot, &hdesc[slot], sizeof(MemberDev<T>), cudaMemcpyHostToDevice);
+    // the items, the slot and the descriptor (its diag fields changed) from
+    // the table staging area, after the member's upload in the stream
+    const size_t bytes = sizeof(FlatItem) * wl.size();
+    sync_stream();  // the member's table upload has left the staging area
+    char* st = stage_tab.get(bytes + sizeof(MemberDev<T>) + 16);
+    std::memcpy(st, wl.data(), bytes);
+    std::memcpy(st + bytes, &hdesc[slot], sizeof(MemberDev<T>));
+    std::memcpy(st + bytes + sizeof(MemberDev<T>), &slot, sizeof(int));
+    cudaError_t e = cudaMemcpyAsync(d_idl, st, bytes, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_mem + slot, st + bytes, sizeof(MemberDev<T>), cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_islot, st + bytes + sizeof(MemberDev<T>), sizeof(int), cudaMemcpyHostToDevice, stream);
     DiagArgs d;
     d.slot = old_;
     d.count_step = 0;  // the initial diag is not a step
-    d.partials = dpart;
+    d.partials = d_ipart;
     d.diag = d_diag;
     d.beta = nullptr;
     d.steps = d_steps;
     d.nan_step = d_nan;
-    int rc = e == cudaSuccess ? launch_diag<T>(d_mem, dwl, (int)wl.size(), dslot, 1, d, stream) : GDC_E_CUDA;
+    int rc = e == cudaSuccess ? launch_diag<T>(d_mem, d_idl, (int)wl.size(), d_islot, 1, d, stream) : GDC_E_CUDA;
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
-    cudaFree(dwl);
-    cudaFree(dpart);
-    cudaFree(dslot);
     hdesc[slot].dbase = saved.dbase;
     hdesc[slot].dcount = saved.dcount;
     if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("initial diag", e));

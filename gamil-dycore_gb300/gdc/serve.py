@@ -1,12 +1,15 @@
 """Forecast serving with continuous batching on one GPU.
 
-Requests (a grid, a forecast length and an arrival time) are admitted into
-one ``gdc.Batch`` as they arrive and as free device memory allows
-(``gdc_batch_add`` refuses a member that would leave less than
-``reserve_bytes`` free); their state stays resident on the device and every
-tick advances all resident members together in the batched step.  A member
-that reaches its length is read back (optionally), removed, and its memory
-serves the next request.  Time to completion is measured from arrival.
+Requests (a grid, a forecast length and an arrival time) are admitted as
+they arrive and as free device memory allows (``gdc_batch_add`` refuses a
+member that would leave less than ``reserve_bytes`` free) into the batch of
+their grid's subcycle count -- one ``gdc.Batch`` per count, each on its own
+CUDA stream, so that every member runs the fast subcycles its grid needs
+and the batches' steps overlap on the device; their state stays resident
+and every tick advances all resident members together in the batched
+steps.  A member that reaches its length is read back (optionally),
+removed, and its memory serves the next request.  Time to completion is
+measured from arrival.
 
 The reference has no serving path: this loop is built on the batch engine's
 C ABI (``gdc_batch_add / _step / _sync / _member_info / _remove``), and the
@@ -72,14 +75,18 @@ def poisson_stream(n: int = 2000, rate: float = 20.0, seed: int = 0, grids=(180,
     return out
 
 
-def serving_scheme(precision: int = FP32):
-    """csp2 with 8 fast subcycles: the batch shares one subcycle count, and
-    at 1440x721 (dt 60 s, 20 filtered rows per pole) 6 subcycles exceed the
-    fast-wave CFL limit next to the filtered rows (the seeded state goes NaN
-    after about 1.3 model days); 8 keep it stable."""
-    return default_params(num_lon=360, num_lat=181, time_step_size=240.0, subcycles=8, split_scheme=SPLIT_CSP2,
-                          qcon_modified=1, use_zonal_tend_filter=1, zonal_tend_filter_cutoff_wavenumber=[4] * 5,
-                          precision=precision)
+# fast subcycles per grid: 6 (the benchmark's scheme) up to 720x361; at
+# 1440x721 (dt 60 s, 20 filtered rows per pole) 6 subcycles exceed the
+# fast-wave CFL limit next to the filtered rows (the seeded state goes NaN
+# after about 1.3 model days) and 8 keep it stable.
+SUBCYCLES = {180: 6, 360: 6, 720: 6, 1440: 8}
+
+
+def serving_scheme(precision: int = FP32, subcycles: int = 6):
+    """csp2 with `subcycles` fast subcycles (the batch of one subcycle class)."""
+    return default_params(num_lon=360, num_lat=181, time_step_size=240.0, subcycles=subcycles,
+                          split_scheme=SPLIT_CSP2, qcon_modified=1, use_zonal_tend_filter=1,
+                          zonal_tend_filter_cutoff_wavenumber=[4] * 5, precision=precision)
 
 
 class InitialStates:
@@ -107,27 +114,53 @@ class InitialStates:
 
 
 class Server:
-    """The request loop.  `batch_factory` builds the engine (a ``gdc.Batch``
-    by default); `steps_per_tick` model steps are taken between admission and
-    completion checks."""
+    """The request loop.  `batch_factory(subcycles)` builds the engine of one
+    subcycle class (a ``gdc.Batch`` by default); `steps_per_tick` model
+    steps are taken between admission and completion checks.  Each batch is
+    autotuned (``gdc_batch_autotune``: its launch schedule, without
+    advancing any member) once it first holds `tune_at` members, and again
+    every `retune_ticks` ticks (0: never again)."""
 
     def __init__(self, precision: int = FP32, steps_per_tick: int = 4, reserve_bytes: int = 2 << 30,
                  max_members: int = 1000, batch_factory=None, initial_states=None, clock=time.perf_counter,
-                 sleep=time.sleep, cuda_stream: int | None = None):
+                 sleep=time.sleep, cuda_stream: int | None = None, tune_at: int = 4, retune_ticks: int = 0):
+        self.precision = precision
         self.steps_per_tick = steps_per_tick
         self.reserve = reserve_bytes
         self.max_members = max_members
         self.clock = clock
         self.sleep = sleep
         self.ics = initial_states or InitialStates()
-        self.batch = batch_factory() if batch_factory else Batch(serving_scheme(precision))
-        if cuda_stream is not None:
-            self.batch.set_stream(cuda_stream)
+        self.factory = batch_factory or (lambda m: Batch(serving_scheme(precision, m)))
+        self.cuda_stream = cuda_stream
+        self.tune_at = tune_at
+        self.retune_ticks = retune_ticks
+        self.batches: dict[int, object] = {}
+        self.tuned: dict[int, int] = {}  # subcycles -> tick of the last tuning
         self.ticks = 0
         self.max_resident = 0
 
+    def batch(self, subcycles: int):
+        if subcycles not in self.batches:
+            b = self.factory(subcycles)
+            if self.cuda_stream is not None:
+                b.set_stream(self.cuda_stream)
+            self.batches[subcycles] = b
+        return self.batches[subcycles]
+
     def close(self):
-        self.batch.close()
+        for b in self.batches.values():
+            b.close()
+        self.batches = {}
+
+    def _maybe_tune(self, resident: dict[int, int]):
+        for m, n in resident.items():
+            last = self.tuned.get(m)
+            due = (last is None and n >= self.tune_at) or (
+                last is not None and self.retune_ticks and self.ticks - last >= self.retune_ticks)
+            if due and hasattr(self.batches[m], "autotune"):
+                self.batches[m].autotune()
+                self.tuned[m] = self.ticks
 
     def run(self, requests: list[Request], keep_results: bool = False, max_wall: float | None = None) -> dict:
         """Serve `requests` (sorted by arrival).  With `max_wall`, arrivals
@@ -135,7 +168,7 @@ class Server:
         admitted requests complete."""
         reqs = sorted(requests, key=lambda r: r.arrival)
         waiting = collections.deque()
-        running: dict[int, Request] = {}
+        running: dict[tuple[int, int], Request] = {}  # (subcycles, member) -> request
         done: list[Request] = []
         nxt = 0
         t0 = self.clock()
@@ -149,19 +182,21 @@ class Server:
             while waiting and len(running) < self.max_members:
                 r = waiting[0]
                 N, M, dt, _, cut = GRIDS[r.grid]
+                m = SUBCYCLES[r.grid]
+                b = self.batch(m)
                 ic = self.ics(r)
                 try:
                     if isinstance(ic, ICSpec):
-                        mid = self.batch.add_ic(N, M, dt, r.nsteps, ic, reserve_bytes=self.reserve, cutoff=cut)
+                        mid = b.add_ic(N, M, dt, r.nsteps, ic, reserve_bytes=self.reserve, cutoff=cut)
                     else:
-                        mid = self.batch.add(N, M, dt, r.nsteps, *ic, reserve_bytes=self.reserve, cutoff=cut)
+                        mid = b.add(N, M, dt, r.nsteps, *ic, reserve_bytes=self.reserve, cutoff=cut)
                 except GdcError as e:
                     if e.code == E_OOM and running:
                         break  # wait for completions to free memory
                     raise
                 r.member = mid
                 r.admitted = self.clock() - t0
-                running[mid] = r
+                running[(m, mid)] = r
                 waiting.popleft()
             self.max_resident = max(self.max_resident, len(running))
             arrivals_left = nxt < len(reqs) and (max_wall is None or reqs[nxt].arrival <= max_wall)
@@ -171,19 +206,25 @@ class Server:
                 if arrivals_left:
                     self.sleep(max(0.0, reqs[nxt].arrival - (self.clock() - t0)))
                 continue
-            self.batch.step(self.steps_per_tick)
-            self.batch.sync()
+            resident = collections.Counter(m for m, _ in running)
+            self._maybe_tune(resident)
+            live = [self.batches[m] for m in resident]
+            for b in live:  # enqueue every class's steps, then wait for all
+                b.step(self.steps_per_tick)
+            for b in live:
+                b.sync()
             self.ticks += 1
             now = self.clock() - t0
-            for mid, r in list(running.items()):
-                steps, fin, nan = self.batch.info(mid)
+            for (m, mid), r in list(running.items()):
+                b = self.batches[m]
+                steps, fin, nan = b.info(mid)
                 if fin or nan >= 0:
                     r.finished = now
                     r.nan_step = nan
                     if keep_results:
-                        r.result = self.batch.get_state(mid)
-                    self.batch.remove(mid)
-                    del running[mid]
+                        r.result = b.get_state(mid)
+                    b.remove(mid)
+                    del running[(m, mid)]
                     done.append(r)
         return summarize(done, len(reqs))
 

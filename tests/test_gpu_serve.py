@@ -12,7 +12,7 @@ pytestmark = pytest.mark.gpu
 
 def solo(req, ics):
     N, M, dt, _, cut = serve.GRIDS[req.grid]
-    b = gdc.Batch(serve.serving_scheme(gdc.FP32))
+    b = gdc.Batch(serve.serving_scheme(gdc.FP32, serve.SUBCYCLES[req.grid]))
     ic = ics(req)
     if isinstance(ic, gdc.ICSpec):
         mid = b.add_ic(N, M, dt, req.nsteps, ic, cutoff=cut)
@@ -31,7 +31,7 @@ def test_served_results_equal_solo_runs(native, device_ic):
     reqs = [serve.Request(rid=k, grid=int(rng.choice([180, 360])), nsteps=int(rng.integers(3, 25)),
                           arrival=0.001 * k) for k in range(10)]
     ics = serve.InitialStates(seed=0, device=device_ic)
-    srv = serve.Server(steps_per_tick=3, initial_states=ics)
+    srv = serve.Server(steps_per_tick=3, initial_states=ics, tune_at=1 << 30)
     stats = srv.run(reqs, keep_results=True)
     srv.close()
     assert stats["completed"] == 10 and stats["nan_members"] == 0

@@ -91,8 +91,8 @@ class FakeBatch:
 def fake_server(capacity=3, steps_per_tick=2):
     clock = FakeClock()
     fb = FakeBatch(clock, capacity=capacity)
-    srv = serve.Server(steps_per_tick=steps_per_tick, batch_factory=lambda: fb, initial_states=lambda r: (0, 0, 0, 0),
-                       clock=clock, sleep=clock.sleep)
+    srv = serve.Server(steps_per_tick=steps_per_tick, batch_factory=lambda m: fb,
+                       initial_states=lambda r: (0, 0, 0, 0), clock=clock, sleep=clock.sleep)
     return srv, fb, clock
 
 
@@ -137,9 +137,37 @@ def test_device_initial_states_go_through_add_ic():
     reqs = [serve.Request(rid=k, grid=360, nsteps=2, arrival=0.0) for k in range(3)]
     clock = FakeClock()
     fb = FakeBatch(clock, capacity=5)
-    srv = serve.Server(steps_per_tick=2, batch_factory=lambda: fb, clock=clock, sleep=clock.sleep)
+    srv = serve.Server(steps_per_tick=2, batch_factory=lambda m: fb, clock=clock, sleep=clock.sleep)
     stats = srv.run(reqs)
     assert stats["completed"] == 3
     assert [sp.kind for sp in fb.specs] == [gdc.IC_SEEDED] * 3
     assert [sp.noise_seed for sp in fb.specs] == [1000, 1001, 1002]
     assert all(sp.noise_sigma == pytest.approx(gdc.G) for sp in fb.specs)
+
+
+def test_each_grid_runs_in_the_batch_of_its_subcycle_count():
+    """180..720 members share the 6-subcycle batch, 1440x721 members the
+    8-subcycle one; both batches step every tick; each is tuned once it
+    holds `tune_at` members."""
+    clock = FakeClock()
+    made = {}
+
+    class Tunable(FakeBatch):
+        tunes = 0
+
+        def autotune(self):
+            self.tunes += 1
+            return 16, 64, 1.0
+
+    def factory(m):
+        made[m] = Tunable(clock, capacity=10)
+        return made[m]
+
+    reqs = [serve.Request(rid=k, grid=g, nsteps=4, arrival=0.0) for k, g in enumerate([180, 1440, 720, 1440, 360])]
+    srv = serve.Server(steps_per_tick=2, batch_factory=factory, initial_states=lambda r: (0, 0, 0, 0),
+                       clock=clock, sleep=clock.sleep, tune_at=2)
+    stats = srv.run(reqs)
+    assert stats["completed"] == 5 and set(made) == {6, 8}
+    assert sorted(N for _, N, _ in made[6].adds) == [180, 360, 720] and len(made[8].adds) == 2
+    assert made[6].tunes == 1 and made[8].tunes == 1
+    assert serve.SUBCYCLES == {180: 6, 360: 6, 720: 6, 1440: 8}
