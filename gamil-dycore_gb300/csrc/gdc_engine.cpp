@@ -209,6 +209,13 @@ class Batch final : public BatchIface {
     std::memset(hdesc.data(), 0, sizeof(MemberDev<T>) * kSlots);
     set_tile(0, 0);
     cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, P.device);
+    // Whether kernels may read pageable host memory through the host's page
+    // tables (a coherent CPU-GPU link, as on Grace): admission then reads
+    // the caller's arrays in place instead of staging them.
+    int pma = 0, pma_host = 0;
+    cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, P.device);
+    cudaDeviceGetAttribute(&pma_host, cudaDevAttrPageableMemoryAccessUsesHostPageTables, P.device);
+    host_direct = pma == 1 && pma_host == 1;
     e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return fail(GDC_E_CUDA, cuda_msg("init", e));
     return GDC_OK;
@@ -407,29 +414,40 @@ class Batch final : public BatchIface {
     // them as given (state(1)%u, %v in the reference), not re-derived.
     const size_t full = (size_t)M * N, half = (size_t)Mh * N, words = 3 * full + half;
     r.ic_ld = ld;
-    r.ic_u.assign(u, u + (size_t)ld * (M + 4));
-    r.ic_v.assign(v, v + (size_t)ld * (Mh + 4));
-    double* hu = reinterpret_cast<double*>(stage_ic.get(words * sizeof(double)));
-    double* hv = hu + full;
-    double* hg = hv + half;
-    double* hh = hg + full;
-    for (int j = 0; j < M; ++j) {
-      const size_t src = (size_t)(j + 2) * ld + 2, dst = (size_t)j * N;
-      std::memcpy(hu + dst, u + src, N * sizeof(double));
-      std::memcpy(hg + dst, gd + src, N * sizeof(double));
-      std::memcpy(hh + dst, ghs + src, N * sizeof(double));
-      if (j < Mh) std::memcpy(hv + dst, v + src, N * sizeof(double));
+    if (sizeof(T) == 8) {  // FP64 read-back of the initial level returns these as given
+      r.ic_u.assign(u, u + (size_t)ld * (M + 4));
+      r.ic_v.assign(v, v + (size_t)ld * (Mh + 4));
     }
-    cudaError_t e = ensure_tmp(words);
+    cudaError_t e = cudaSuccess;
     const int lvl = old_;
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(d_ictmp, hu, words * sizeof(double), cudaMemcpyHostToDevice, stream);
-    if (e == cudaSuccess) {
-      double* du = d_ictmp;
-      double* dv = du + full;
-      double* dg = dv + half;
-      if (launch_ic_iap<T>(d_mem, slot, lvl, N, M, du, dv, dg, dg + full, stream) != GDC_OK)
+    if (host_direct) {
+      // The device reads the caller's padded arrays in place (their
+      // interior, rows ld apart) over the coherent host link.
+      const size_t o = (size_t)2 * ld + 2;
+      if (launch_ic_iap<T>(d_mem, slot, lvl, N, M, u + o, v + o, gd + o, ghs + o, ld, stream) != GDC_OK)
         e = cudaGetLastError();
+    } else {
+      double* hu = reinterpret_cast<double*>(stage_ic.get(words * sizeof(double)));
+      double* hv = hu + full;
+      double* hg = hv + half;
+      double* hh = hg + full;
+      for (int j = 0; j < M; ++j) {
+        const size_t src = (size_t)(j + 2) * ld + 2, dst = (size_t)j * N;
+        std::memcpy(hu + dst, u + src, N * sizeof(double));
+        std::memcpy(hg + dst, gd + src, N * sizeof(double));
+        std::memcpy(hh + dst, ghs + src, N * sizeof(double));
+        if (j < Mh) std::memcpy(hv + dst, v + src, N * sizeof(double));
+      }
+      e = ensure_tmp(words);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_ictmp, hu, words * sizeof(double), cudaMemcpyHostToDevice, stream);
+      if (e == cudaSuccess) {
+        double* du = d_ictmp;
+        double* dv = du + full;
+        double* dg = dv + half;
+        if (launch_ic_iap<T>(d_mem, slot, lvl, N, M, du, dv, dg, dg + full, N, stream) != GDC_OK)
+          e = cudaGetLastError();
+      }
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_uvslot + slot, &lvl, sizeof(int), cudaMemcpyHostToDevice, stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
@@ -494,7 +512,7 @@ class Batch final : public BatchIface {
     const int lvl = old_;
     e = cudaMemcpyAsync(dt_tab, tables.data(), tables.size() * sizeof(double), cudaMemcpyHostToDevice, stream);
     int rc = e == cudaSuccess ? ic_generate(spec, N, M, dt_tab, scratch, du, dv, dg, dh, stream) : GDC_E_CUDA;
-    if (rc == GDC_OK) rc = launch_ic_iap<T>(d_mem, slot, lvl, N, M, du, dv, dg, dh, stream);
+    if (rc == GDC_OK) rc = launch_ic_iap<T>(d_mem, slot, lvl, N, M, du, dv, dg, dh, N, stream);
     if (rc == GDC_OK)
       rc = cudaMemcpyAsync(d_uvslot + slot, &lvl, sizeof(int), cudaMemcpyHostToDevice, stream) == cudaSuccess
                ? GDC_OK
@@ -818,16 +836,22 @@ class Batch final : public BatchIface {
     const double* hu = ov + nh;
     const double* hv = hu + n;
     const double* sg = hv + nh;
+    // Each element of the padded array written once: zero latitude-halo
+    // rows, then per interior row its values, periodic longitude halo and
+    // zero padding past N + 4.
     auto put = [&](double* f, int rows, const double* src) {
       if (!f) return;
-      std::memset(f, 0, sizeof(double) * (size_t)ld * (rows + 4));
-      for (int j = 0; j < rows; ++j) std::memcpy(f + (size_t)(j + 2) * ld + 2, src + (size_t)j * N, N * sizeof(double));
-      for (int j = 0; j < rows + 4; ++j) {
-        double* row = f + (size_t)j * ld;
-        row[0] = row[N];
-        row[1] = row[N + 1];
-        row[N + 2] = row[2];
-        row[N + 3] = row[3];
+      std::memset(f, 0, sizeof(double) * (size_t)ld * 2);
+      std::memset(f + (size_t)(rows + 2) * ld, 0, sizeof(double) * (size_t)ld * 2);
+      for (int j = 0; j < rows; ++j) {
+        double* row = f + (size_t)(j + 2) * ld;
+        const double* sr = src + (size_t)j * N;
+        std::memcpy(row + 2, sr, N * sizeof(double));
+        row[0] = sr[N - 2];
+        row[1] = sr[N - 1];
+        row[N + 2] = sr[0];
+        row[N + 3] = sr[1];
+        if (ld > N + 4) std::memset(row + N + 4, 0, sizeof(double) * (ld - N - 4));
       }
     };
     put(gd, M, hg);
@@ -1224,6 +1248,7 @@ class Batch final : public BatchIface {
   // the update's loads land on its critical path), so off by default.
   bool fuse_final = false;
   int num_sms = 152;
+  bool host_direct = false;  // kernels read pageable host memory (see init)
   // With strips, the whole-row tasks run on a second stream, concurrently
   // with the strips over the ordinary rows.
   cudaStream_t side = nullptr;

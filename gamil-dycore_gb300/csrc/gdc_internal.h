@@ -342,11 +342,12 @@ int launch_stage_strips(const MemberDev<T>* mem, const WorkItem* strips, int nst
                         void* stream);
 // History output of member `slot` at level `lvl` into device FP64 buffers
 // (num_lat x num_lon each; vor num_lat - 1 rows).
-// iap_transform of a device initial condition into member `slot`'s level
-// `lvl`, its given u, v and ghs (src/types_mod.F90:399-426).
+// iap_transform of an FP64 initial condition into member `slot`'s level
+// `lvl`, its given u, v and ghs (src/types_mod.F90:399-426); inputs point at
+// element (0, 0), rows `ld` apart.
 template <typename T>
 int launch_ic_iap(const MemberDev<T>* mem, int slot, int lvl, int N, int M, const double* u, const double* v,
-                  const double* gd, const double* ghs, void* stream);
+                  const double* gd, const double* ghs, int ld, void* stream);
 // Member `slot`'s level `lvl` in FP64, compact: gd [M N], u [M N],
 // v [Mh N], iap u [M N], iap v [Mh N], iap gd [M N]; u, v derived
 // (uv_mode 0), the given ones (1) or not written (2).

@@ -2384,14 +2384,17 @@ int launch_history(const MemberDev<T>* mem, int slot, int lvl, int given, int nu
 }
 
 // iap_transform (src/types_mod.F90:399-426) of an FP64 initial condition
-// already in device memory (compact, lon fastest) into member `slot`'s
-// time level `lvl`, with the FP32 compensation words where the level has
-// them; the condition's own u, v become the level's given u, v.  FP64
+// into member `slot`'s time level `lvl`, with the FP32 compensation words
+// where the level has them; the condition's own u, v become the level's
+// given u, v.  The inputs point at element (0, 0) of rows `ld` apart
+// (compact device arrays: ld = N; the caller's padded host arrays, read in
+// place where the device reads pageable host memory: their interior).  FP64
 // arithmetic with explicit roundings, as on the host.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
     ic_iap_kernel(const MemberDev<T>* __restrict__ mems, int slot, int lvl, const double* __restrict__ u,
-                  const double* __restrict__ v, const double* __restrict__ gd, const double* __restrict__ ghs) {
+                  const double* __restrict__ v, const double* __restrict__ gd, const double* __restrict__ ghs,
+                  int ld) {
   const MemberDev<T>& d = mems[slot];
   const int N = d.N, Mh = d.Mh, n = d.M * N;
   auto put = [](T* hi, T* lo, int q, double x) {
@@ -2401,25 +2404,26 @@ __global__ void __launch_bounds__(kThreads)
   };
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
     const int j = q / N, i = q - j * N;
-    const double g = gd[q], sg = __dsqrt_rn(g);
+    const size_t r = (size_t)j * ld + i;
+    const double g = gd[r], sg = __dsqrt_rn(g);
     put(d.st[lvl][F_GD], d.lo[lvl][F_GD], q, g);
-    d.ghs[q] = T(ghs[q]);
-    const int qp = i + 1 == N ? q + 1 - N : q + 1;
-    put(d.st[lvl][F_IU], d.lo[lvl][F_IU], q, __dmul_rn(__dmul_rn(0.5, __dadd_rn(sg, __dsqrt_rn(gd[qp]))), u[q]));
-    d.given_u[q] = T(u[q]);
+    d.ghs[q] = T(ghs[r]);
+    const size_t rp = i + 1 == N ? r + 1 - N : r + 1;
+    put(d.st[lvl][F_IU], d.lo[lvl][F_IU], q, __dmul_rn(__dmul_rn(0.5, __dadd_rn(sg, __dsqrt_rn(gd[rp]))), u[r]));
+    d.given_u[q] = T(u[r]);
     if (j < Mh) {
       put(d.st[lvl][F_IV], d.lo[lvl][F_IV], q,
-          __dmul_rn(__dmul_rn(0.5, __dadd_rn(sg, __dsqrt_rn(gd[q + N]))), v[q]));
-      d.given_v[q] = T(v[q]);
+          __dmul_rn(__dmul_rn(0.5, __dadd_rn(sg, __dsqrt_rn(gd[r + ld]))), v[r]));
+      d.given_v[q] = T(v[r]);
     }
   }
 }
 
 template <typename T>
 int launch_ic_iap(const MemberDev<T>* mem, int slot, int lvl, int N, int M, const double* u, const double* v,
-                  const double* gd, const double* ghs, void* stream) {
+                  const double* gd, const double* ghs, int ld, void* stream) {
   const int n = N * M, grid = (n + kThreads - 1) / kThreads;
-  ic_iap_kernel<T><<<grid, kThreads, 0, (cudaStream_t)stream>>>(mem, slot, lvl, u, v, gd, ghs);
+  ic_iap_kernel<T><<<grid, kThreads, 0, (cudaStream_t)stream>>>(mem, slot, lvl, u, v, gd, ghs, ld);
   return check_launch();
 }
 

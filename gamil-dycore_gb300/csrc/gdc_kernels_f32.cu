@@ -13,7 +13,7 @@ template int launch_stage_strips<float>(const MemberDev<float>*, const WorkItem*
 template int launch_history<float>(const MemberDev<float>*, int, int, int, int, double*, double*, double*, double*,
                                    double*, void*);
 template int launch_ic_iap<float>(const MemberDev<float>*, int, int, int, int, const double*, const double*,
-                                 const double*, const double*, void*);
+                                 const double*, const double*, int, void*);
 template int launch_weno<float>(const MemberDev<float>*, const FlatItem*, int, int, const int*, void*);
 template int launch_state_out<float>(const MemberDev<float>*, int, int, int, int, int, double*, void*);
 template int launch_final<float>(const MemberDev<float>*, const FlatItem*, int, const FinalArgs&, void*);

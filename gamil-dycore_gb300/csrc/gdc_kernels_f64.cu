@@ -16,7 +16,7 @@ template int launch_stage_strips<double>(const MemberDev<double>*, const WorkIte
 template int launch_history<double>(const MemberDev<double>*, int, int, int, int, double*, double*, double*, double*,
                                    double*, void*);
 template int launch_ic_iap<double>(const MemberDev<double>*, int, int, int, int, const double*, const double*,
-                                 const double*, const double*, void*);
+                                 const double*, const double*, int, void*);
 template int launch_weno<double>(const MemberDev<double>*, const FlatItem*, int, int, const int*, void*);
 template int launch_state_out<double>(const MemberDev<double>*, int, int, int, int, int, double*, void*);
 template int launch_final<double>(const MemberDev<double>*, const FlatItem*, int, const FinalArgs&, void*);

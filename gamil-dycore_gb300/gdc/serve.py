@@ -75,11 +75,13 @@ def poisson_stream(n: int = 2000, rate: float = 20.0, seed: int = 0, grids=(180,
     return out
 
 
-# fast subcycles per grid: 6 (the benchmark's scheme) up to 720x361; at
-# 1440x721 (dt 60 s, 20 filtered rows per pole) 6 subcycles exceed the
-# fast-wave CFL limit next to the filtered rows (the seeded state goes NaN
-# after about 1.3 model days) and 8 keep it stable.
-SUBCYCLES = {180: 6, 360: 6, 720: 6, 1440: 8}
+# fast subcycles per grid for forecasts of up to 5 days: 6 (the benchmark's
+# scheme) at 180x91 and 360x181 (stable for 5 days); at 720x361 and
+# 1440x721 the fast step dt/6 exceeds the fast-wave CFL limit at the first
+# unfiltered row (gravity-wave Courant number ~1.2 at 5 degrees from the
+# pole; the seeded 1440x721 state goes NaN after about 1.3 model days) and 8
+# keep them stable.
+SUBCYCLES = {180: 6, 360: 6, 720: 8, 1440: 8}
 
 
 def serving_scheme(precision: int = FP32, subcycles: int = 6):
@@ -247,4 +249,6 @@ def summarize(done: list[Request], offered: int) -> dict:
         "span_s": float(span),
         "gpt_steps_per_s": float(work / span) if span > 0 else float("nan"),
         "nan_members": int(sum(1 for r in done if r.nan_step >= 0)),
+        "nan_members_by_grid": {str(g): int(sum(1 for r in done if r.nan_step >= 0 and r.grid == g))
+                                for g in sorted({r.grid for r in done})},
     }
