@@ -418,12 +418,44 @@ __device__ void tile_combine(const MemberDev<T>& md, const StageArgs& a, int mem
 // After the copies: iap gd, then u on full rows j0..j0+R (local 1..R+1;
 // from local 0 when the stencil also needs row j0-1), v on half rows
 // j0-1..j0+R (local 0..R+1), columns i0-1..i0+W (local 0..W+1).
+// Local tile rows (inclusive) on which iap gd, u and v are derived; an
+// empty range (lo > hi) derives none.  Whole tiles derive every row their
+// stencils may read; a whole-row task for one field derives only the rows
+// that field's stencil reads (row_task_rows).
+struct DeriveRows {
+  int ig0 = 0, ig1 = 1 << 20, u0 = 0, u1 = 1 << 20, v0 = 0, v1 = 1 << 20;
+};
+
+// A one-row tile (the task's row at local row 1) computing the tendency of
+// field f alone (f < 0: all three), pass `pass` (src/dycore_mod.F90:
+// 367-598): du reads u on its row (and v on the half rows around it in the
+// advection), dv reads u on its row and the next and v on three half rows,
+// dgd only iap gd.
+__device__ inline DeriveRows row_task_rows(int pass, int f) {
+  DeriveRows d;
+  if (f < 0) return d;
+  if (f == F_GD) {
+    d.ig0 = 0, d.ig1 = 2, d.u0 = 1, d.u1 = 0, d.v0 = 1, d.v1 = 0;
+  } else if (f == F_IU) {
+    if (pass == kFastPass)
+      d.ig0 = 1, d.ig1 = 1, d.u0 = 1, d.u1 = 1, d.v0 = 1, d.v1 = 0;
+    else
+      d.ig0 = 0, d.ig1 = 2, d.u0 = 1, d.u1 = 1, d.v0 = 0, d.v1 = 1;
+  } else {
+    if (pass == kFastPass)
+      d.ig0 = 1, d.ig1 = 2, d.u0 = 1, d.u1 = 2, d.v0 = 1, d.v1 = 0;
+    else
+      d.ig0 = 0, d.ig1 = 3, d.u0 = 1, d.u1 = 2, d.v0 = 0, d.v1 = 2;
+  }
+  return d;
+}
+
 template <typename T, int R, int W>
 __device__ void tile_derive(const MemberDev<T>& md, Tile<T, R, W>& t, bool u_halo_row = false,
-                            bool given = false, bool want_v = true, bool want_u = true) {
+                            bool given = false, bool want_v = true, DeriveRows rows = DeriveRows()) {
   using TL = Tile<T, R, W>;
   const int M = md.M, Mh = md.Mh;
-  const int urow0 = u_halo_row ? 0 : 1;
+  const int urow0 = max(u_halo_row ? 0 : 1, rows.u0);
   constexpr int DW = W + 2, ND = (R + 2) * (W + 2);
   cp_async_wait_all();
   __syncthreads();
@@ -436,18 +468,22 @@ __device__ void tile_derive(const MemberDev<T>& md, Tile<T, R, W>& t, bool u_hal
       if (rr > t.vrows + 1 || cc > t.vcols + 1) continue;
       const int j = t.j0 - 1 + rr;
       const T g0 = sqrt(t.gd[p]);
-      t.ig[p] = g0;
+      if (rr >= rows.ig0 && rr <= rows.ig1) t.ig[p] = g0;
       if (given) continue;
       T uu = 0, vv = 0;
-      if (want_u && rr >= urow0 && j >= 1 && j <= M - 2) uu = t.iu[p] * T(2) / (g0 + sqrt(t.gd[p + 1]));
-      if (want_v && j >= 0 && j < Mh) vv = t.iv[p] * T(2) / (g0 + sqrt(t.gd[p + TL::SW]));
+      if (rr >= urow0 && rr <= rows.u1 && j >= 1 && j <= M - 2) uu = t.iu[p] * T(2) / (g0 + sqrt(t.gd[p + 1]));
+      if (want_v && rr >= rows.v0 && rr <= rows.v1 && j >= 0 && j < Mh)
+        vv = t.iv[p] * T(2) / (g0 + sqrt(t.gd[p + TL::SW]));
       t.u[p] = uu;
       t.v[p] = vv;
     }
     __syncthreads();
     return;
   }
-  for (int p = threadIdx.x; p < TL::NS; p += kThreads) t.ig[p] = sqrt(t.gd[p]);
+  for (int p = threadIdx.x; p < TL::NS; p += kThreads) {
+    const int rr = p / TL::SW;
+    if (rr >= rows.ig0 && rr <= rows.ig1) t.ig[p] = sqrt(t.gd[p]);
+  }
   __syncthreads();
   if (given) return;
   for (int q = threadIdx.x; q < ND; q += kThreads) {
@@ -456,8 +492,9 @@ __device__ void tile_derive(const MemberDev<T>& md, Tile<T, R, W>& t, bool u_hal
     const int j = t.j0 - 1 + rr;
     const bool need = rr <= t.vrows + 1 && cc <= t.vcols + 1;
     T uu = 0, vv = 0;
-    if (want_u && need && rr >= urow0 && j >= 1 && j <= M - 2) uu = t.iu[p] * T(2) / (t.ig[p] + t.ig[p + 1]);
-    if (want_v && need && j >= 0 && j < Mh) vv = t.iv[p] * T(2) / (t.ig[p] + t.ig[p + TL::SW]);
+    if (need && rr >= urow0 && rr <= rows.u1 && j >= 1 && j <= M - 2) uu = t.iu[p] * T(2) / (t.ig[p] + t.ig[p + 1]);
+    if (want_v && need && rr >= rows.v0 && rr <= rows.v1 && j >= 0 && j < Mh)
+      vv = t.iv[p] * T(2) / (t.ig[p] + t.ig[p + TL::SW]);
     t.u[p] = uu;
     t.v[p] = vv;
   }
@@ -1599,8 +1636,8 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
       __syncthreads();
       tile_issue(md, gd_in, iu_in, iv_in, t, given, PASS != kSlowPass, fuse ? md.td[TS_NEW] : nullptr);
       if (fuse) tile_combine(md, a, w.member, t, f < 0 ? 7 : (1 << f));
-      // A gd-only task (mass divergence, pole cap) reads no u and no v.
-      tile_derive(md, t, false, given, PASS != kFastPass && f != F_GD, f != F_GD);
+      // only the rows this task's field reads
+      tile_derive(md, t, false, given, PASS != kFastPass, row_task_rows(PASS, f));
       for (int c = threadIdx.x; c < vw; c += blockDim.x) {
         const int p = TR::pos(1, c + 1);
         const int i = c0 + c;
