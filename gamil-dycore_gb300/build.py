@@ -20,6 +20,10 @@ ROOT = PKG.parent
 INCLUDE = ROOT / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Tile shapes of the stage kernel (rows x columns) per real type; the
+# engine's tile_shape_supported accepts exactly these.
+STAGE_SHAPES = {"f64": [(16, 64), (8, 64), (8, 32), (4, 128), (4, 32)],
+                "f32": [(16, 64), (8, 64), (8, 32), (4, 128)]}
 
 
 def _cuda_home() -> Path:
@@ -59,17 +63,25 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     lib = OUT / "libgdc.so"
     headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [INCLUDE / "gdc.h"]
     cu = [CSRC / "gdc_kernels_f64.cu", CSRC / "gdc_kernels_f32.cu", CSRC / "gdc_noalloc.cu", CSRC / "gdc_ic.cu"]
+    shape_src = CSRC / "gdc_stage_shape.cu"
     cpp = [CSRC / "gdc_engine.cpp", CSRC / "gdc_host.cpp"]
-    if force or _stale(lib, cu + cpp + headers):
+    # (stem, source, defines): the stage kernels compile once per real type
+    # and tile shape, in parallel with the other units.
+    units = [(src.stem, src, []) for src in cu]
+    for real, tag in (("double", "f64"), ("float", "f32")):
+        for r, w in STAGE_SHAPES[tag]:
+            units.append((f"gdc_stage_{r}x{w}_{tag}", shape_src,
+                          [f"-DGDC_REAL={real}", f"-DGDC_TILE_R={r}", f"-DGDC_TILE_W={w}"]))
+    if force or _stale(lib, cu + [shape_src] + cpp + headers):
         cmds, objs = [], []
-        for src in cu:
-            obj = OUT / (src.stem + ".o")
+        for stem, src, defs in units:
+            obj = OUT / (stem + ".o")
             objs.append(obj)
             # The FP64 units keep the reference's rounding: no FMA contraction.
-            # The FP32 unit uses fast single-precision division and square
+            # The FP32 units use fast single-precision division and square
             # root (fast math affects single precision only).
-            fmad = ["--fmad=false"] if src.stem.endswith(("_f64", "_noalloc", "_ic")) else ["--use_fast_math"]
-            cmds.append([nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", *fmad, "-Xcompiler",
+            fmad = ["--fmad=false"] if stem.endswith(("_f64", "_noalloc", "_ic")) else ["--use_fast_math"]
+            cmds.append([nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", *fmad, *defs, "-Xcompiler",
                          "-fPIC,-ffp-contract=off", f"-I{INCLUDE}", "-c", str(src), "-o", str(obj)])
         for src in cpp:
             obj = OUT / (src.stem + ".o")

@@ -1567,17 +1567,16 @@ struct StageOcc {
   static constexpr int kMinBlocks = sizeof(T) == 4 ? GDC_STAGE_BLOCKS : 2;
 };
 
+// One work item of a stage (a bulk tile or a whole-row task), by the block.
 template <typename T, int PASS, int ADV, int R, int W>
-__global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
-    stage_kernel(const MemberDev<T>* __restrict__ mems, const WorkItem* __restrict__ wl, StageArgs a,
-                 int staging_words, int max_n) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void stage_item(const MemberDev<T>* __restrict__ mems, const WorkItem w,
+                                           const StageArgs& a, unsigned char* smem_raw, int staging_words,
+                                           int max_n) {
   T* staging = reinterpret_cast<T*>(smem_raw);  // bulk tile, or the row task's tile, then:
   T* rows = staging + row_task_words<T>();      // 3 * max_n (row tasks)
   T* coefs = rows + 3 * max_n;                  // kMaxKeep
   T* tw = coefs + kMaxKeep;                     // 2 * max_n twiddles
   T* redT = staging + staging_words;            // 64, then 64 doubles
-  const WorkItem w = wl[blockIdx.x];
   // The member descriptor is read in place (read-only, L1-cached): copying
   // it to shared memory cost a barrier per block.
   const MemberDev<T>& md = mems[w.member];
@@ -1688,6 +1687,15 @@ __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
       pp[3] = (double)s2.c;
     }
   }
+}
+
+// A stage launch: one block per work item.
+template <typename T, int PASS, int ADV, int R, int W>
+__global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
+    stage_kernel(const MemberDev<T>* __restrict__ mems, const WorkItem* __restrict__ wl, StageArgs a,
+                 int staging_words, int max_n) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  stage_item<T, PASS, ADV, R, W>(mems, wl[blockIdx.x], a, smem_raw, staging_words, max_n);
 }
 
 // Warp strips, one per warp (items cover every row of their members).
@@ -2343,9 +2351,17 @@ static int launch_stage_t(const MemberDev<T>* mem, const WorkItem* wl, int nwork
   return check_launch();
 }
 
+// One tile shape's stage kernels (three passes x two advection schemes).
+// Each (real type, shape) pair is instantiated in a translation unit of its
+// own (gdc_stage_shape.cu built once per pair) so that the library's
+// kernels compile in parallel.
 template <typename T, int R, int W>
-static int launch_stage_shape(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int adv, int max_n,
-                              const StageArgs& a, cudaStream_t s) {
+int launch_stage_shape(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int adv, int max_n,
+                       const StageArgs& a, cudaStream_t s);
+#ifdef GDC_STAGE_SHAPE_UNIT
+template <typename T, int R, int W>
+int launch_stage_shape(const MemberDev<T>* mem, const WorkItem* wl, int nwork, int adv, int max_n,
+                       const StageArgs& a, cudaStream_t s) {
 #define GDC_DISPATCH(P, A) \
   if (a.pass == P && adv == A) return launch_stage_t<T, P, A, R, W>(mem, wl, nwork, max_n, a, s);
   GDC_DISPATCH(kAllPass, GDC_ADV_CENTER_DIFF)
@@ -2357,6 +2373,7 @@ static int launch_stage_shape(const MemberDev<T>* mem, const WorkItem* wl, int n
 #undef GDC_DISPATCH
   return GDC_E_CONFIG;
 }
+#endif
 
 // WENO members use 8x32 tiles only (one instantiation per pass; the fast
 // pass has no advection and runs the centred kernel).
