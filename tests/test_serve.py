@@ -146,8 +146,8 @@ def test_device_initial_states_go_through_add_ic():
 
 
 def test_each_grid_runs_in_the_batch_of_its_subcycle_count():
-    """180x91 and 360x181 members share the 6-subcycle batch, 720x361 and
-    1440x721 members the 8-subcycle one; both batches step every tick; each
+    """180x91 and 360x181 members share the 6-subcycle batch, 1440x721
+    members run in the 10-subcycle one; both batches step every tick; each
     is tuned once it holds `tune_at` members."""
     clock = FakeClock()
     made = {}
@@ -167,7 +167,7 @@ def test_each_grid_runs_in_the_batch_of_its_subcycle_count():
     srv = serve.Server(steps_per_tick=2, batch_factory=factory, initial_states=lambda r: (0, 0, 0, 0),
                        clock=clock, sleep=clock.sleep, tune_at=2)
     stats = srv.run(reqs)
-    assert stats["completed"] == 5 and set(made) == {6, 8}
-    assert sorted(N for _, N, _ in made[6].adds) == [180, 180, 360] and len(made[8].adds) == 2
-    assert made[6].tunes == 1 and made[8].tunes == 1
-    assert serve.SUBCYCLES == {180: 6, 360: 6, 720: 8, 1440: 8}
+    assert stats["completed"] == 5 and set(made) == {6, 10}
+    assert sorted(N for _, N, _ in made[6].adds) == [180, 180, 360] and len(made[10].adds) == 2
+    assert made[6].tunes == 1 and made[10].tunes == 1
+    assert serve.SUBCYCLES == {180: 6, 360: 6, 720: 8, 1440: 10}
