@@ -239,7 +239,8 @@ def summarize(done: list[Request], offered: int) -> dict:
         return {"completed": 0, "offered": offered}
     lat = np.array([r.latency for r in done])
     wait = np.array([r.admitted - r.arrival for r in done])
-    work = sum(r.points * r.nsteps for r in done)
+    # a member stopped by a NaN did only the steps before it
+    work = sum(r.points * (r.nan_step if r.nan_step >= 0 else r.nsteps) for r in done)
     span = max(r.finished for r in done) - min(r.arrival for r in done)
     return {
         "completed": len(done),
@@ -254,4 +255,6 @@ def summarize(done: list[Request], offered: int) -> dict:
         "nan_members": int(sum(1 for r in done if r.nan_step >= 0)),
         "nan_members_by_grid": {str(g): int(sum(1 for r in done if r.nan_step >= 0 and r.grid == g))
                                 for g in sorted({r.grid for r in done})},
+        "nan_requests": [{"rid": r.rid, "grid": r.grid, "nsteps": r.nsteps, "nan_step": r.nan_step}
+                         for r in done if r.nan_step >= 0],
     }

@@ -171,3 +171,25 @@ def test_each_grid_runs_in_the_batch_of_its_subcycle_count():
     assert sorted(N for _, N, _ in made[6].adds) == [180, 180, 360] and len(made[10].adds) == 2
     assert made[6].tunes == 1 and made[10].tunes == 1
     assert serve.SUBCYCLES == {180: 6, 360: 6, 720: 8, 1440: 10}
+
+
+def test_nan_member_is_reported_and_counted_to_its_stop():
+    """A member whose mass or energy turns NaN is stopped and listed; its
+    grid-point steps count only the steps it did."""
+    clock = FakeClock()
+
+    class NanAt2(FakeBatch):
+        def info(self, mid):
+            s, n = self.members[mid]
+            if mid == 1 and s >= 2:
+                return s, False, 2
+            return s, s >= n, -1
+
+    fb = NanAt2(clock, capacity=4)
+    reqs = [serve.Request(rid=k, grid=180, nsteps=6, arrival=0.0) for k in range(3)]
+    srv = serve.Server(steps_per_tick=2, batch_factory=lambda m: fb, initial_states=lambda r: (0, 0, 0, 0),
+                       clock=clock, sleep=clock.sleep)
+    st = srv.run(reqs)
+    assert st["completed"] == 3 and st["nan_members"] == 1
+    assert st["nan_requests"] == [{"rid": 1, "grid": 180, "nsteps": 6, "nan_step": 2}]
+    assert st["gpt_steps"] == reqs[0].points * (6 + 2 + 6)
