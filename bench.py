@@ -232,7 +232,7 @@ def stage_words_per_launch(subcycles=SUBCYCLES, fused=True):
 def apply_schedule(b, sched):
     if sched:
         b.set_tile(*sched["tile"])
-        b.set_schedule(sched["split_rows"], sched["fuse_final"])
+        b.set_schedule(sched["split_rows"], sched["fuse_final"], sched["pair_rows"])
 
 
 def e2e_batch(gdc, torch, members, steps, precision, sched=None):
@@ -621,7 +621,8 @@ def run_ours(args, rank, world, dist):
                        parallelism=f"replicas x{world}",
                        schedule=f"autotuned: tiles {sched['tile'][0]}x{sched['tile'][1]}, "
                                 f"row tasks {('auto', 'whole', 'split')[sched['split_rows'] + 1]}, "
-                                f"final update {'fused' if sched['fuse_final'] else 'launched'}"),
+                                f"final update {'fused' if sched['fuse_final'] else 'launched'}"
+                                f"{', row tasks split over block pairs' if sched['pair_rows'] else ''}"),
         "clocks": clocks,
         "e2e": {"value": world * e2e_gpt / (e2e_ms / 1e3), "unit": "grid-pt-steps/s",
                 "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps},

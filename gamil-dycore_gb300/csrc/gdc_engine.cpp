@@ -165,8 +165,8 @@ struct BatchIface {
   virtual int diag(int id, double* m, double* e, double* b) = 0;
   virtual int active(int* n) = 0;
   virtual int set_tile(int r, int c) = 0;
-  virtual int set_schedule(int split_rows, int fuse_final) = 0;
-  virtual int get_schedule(int* r, int* c, int* split, int* fuse) = 0;
+  virtual int set_schedule(int split_rows, int fuse_final, int pair_rows) = 0;
+  virtual int get_schedule(int* r, int* c, int* split, int* fuse, int* pair) = 0;
   virtual int autotune(int* r, int* c, double* ms) = 0;
   virtual int profile(int n, double* ms, long long* launches) = 0;
   virtual int set_stream(void* s) = 0;
@@ -904,11 +904,13 @@ class Batch final : public BatchIface {
     return GDC_OK;
   }
 
-  int set_schedule(int split, int fuse) override {
-    if (split < -1 || split > 1 || fuse < 0 || fuse > 1)
-      return fail(GDC_E_CONFIG, "set_schedule: split_rows must be -1, 0 or 1 and fuse_final 0 or 1");
+  int set_schedule(int split, int fuse, int pair) override {
+    if (split < -1 || split > 1 || fuse < 0 || fuse > 1 || pair < -1 || pair > 1)
+      return fail(GDC_E_CONFIG,
+                  "set_schedule: split_rows and pair_rows must be -1, 0 or 1 and fuse_final 0 or 1");
     split_mode = split;
     fuse_final = fuse != 0;
+    pair_mode = pair;
     dirty = true;
     return GDC_OK;
   }
@@ -993,18 +995,20 @@ class Batch final : public BatchIface {
     }
     const std::vector<MemberRec> saved_recs = recs;
     const int saved_old = old_, saved_new = new_;
-    std::array<int, 4> pick = {tile_r, tile_c, split_mode, fuse_final ? 1 : 0};
+    std::array<int, 5> pick = {tile_r, tile_c, split_mode, fuse_final ? 1 : 0, pair_mode};
     // No member may finish while the candidates are timed.
     for (int sl : active_slots) recs[sl].nsteps = recs[sl].steps_done + (1LL << 40);
 
     // --- time the candidates
-    std::vector<std::array<int, 4>> cand;  // rows, cols, split, fuse
+    std::vector<std::array<int, 5>> cand;  // rows, cols, split, fuse, pair
     const int shapes[][2] = {{16, 64}, {8, 64}, {8, 32}, {4, 128}, {4, 32}, {16, 30}};
     for (auto& sh : shapes) {
       const bool st = strip_shape_supported(sh[0], sh[1]);
       if (!st && !tile_shape_supported(sh[0], sh[1], sizeof(T) == 8)) continue;
       for (int split = 0; split <= 1; ++split)
-        for (int fuse = 0; fuse <= (st ? 0 : 1); ++fuse) cand.push_back({sh[0], sh[1], split, fuse});
+        for (int fuse = 0; fuse <= (st ? 0 : 1); ++fuse)
+          for (int pair = 0; pair <= (sizeof(T) == 4 || st || fuse || weno() ? 0 : 1); ++pair)
+            cand.push_back({sh[0], sh[1], split, fuse, pair});
     }
     const int reps = 3;
     cudaEvent_t e0, e1;
@@ -1014,7 +1018,7 @@ class Batch final : public BatchIface {
     int rc = GDC_OK;
     for (auto& c : cand) {
       rc = set_tile(c[0], c[1]);
-      if (rc == GDC_OK) rc = set_schedule(c[2], c[3]);
+      if (rc == GDC_OK) rc = set_schedule(c[2], c[3], c[4]);
       if (rc == GDC_OK) rc = step(2);  // build, capture both time-level parities
       std::vector<float> t;
       for (int k = 0; k < reps && rc == GDC_OK; ++k) {
@@ -1068,7 +1072,7 @@ class Batch final : public BatchIface {
     old_ = saved_old;
     new_ = saved_new;
     set_tile(pick[0], pick[1]);
-    set_schedule(pick[2], pick[3]);
+    set_schedule(pick[2], pick[3], pick[4]);
     invalidate_graphs();
     dirty = true;
     if (rc) return rc;
@@ -1079,11 +1083,14 @@ class Batch final : public BatchIface {
     return GDC_OK;
   }
 
-  int get_schedule(int* r, int* c, int* split, int* fuse) override {
+  int get_schedule(int* r, int* c, int* split, int* fuse, int* pair) override {
+    if (dirty)
+      if (int rc = rebuild()) return rc;
     if (r) *r = tile_r;
     if (c) *c = tile_c;
     if (split) *split = split_mode;
     if (fuse) *fuse = fuse_final ? 1 : 0;
+    if (pair) *pair = pair_rows ? 1 : 0;
     return GDC_OK;
   }
 
@@ -1143,6 +1150,7 @@ class Batch final : public BatchIface {
     StageArgs a = base_args(pass);
     a.in_slot = level_of(id);
     a.tout = TS_NEW;
+    a.pair = 0;  // no clusters here: part 0 of a paired row task does it whole
     int nr = 0;
     for (const auto& w : wl) nr += w.kind == 1;
     int rc = GDC_OK;
@@ -1243,6 +1251,12 @@ class Batch final : public BatchIface {
   // critical path); otherwise one task per row stages the row once.
   bool split_rows = sizeof(T) == 8;
   int split_mode = -1;     // -1 automatic (above), 0 whole rows, 1 split by field
+  // Whole-row tasks split over the two blocks of a cluster (-1 automatic:
+  // FP64 launches with at most two items per SM, where the filtered rows'
+  // FP64 sums are the critical path; 0 off; 1 on).  FP64 tiles only, not
+  // with a fused final update.
+  int pair_mode = -1;
+  bool pair_rows = false;
   // predict_correct's update formed in the next one's first stage: correct
   // and tested, but measured slower (the first stage is latency-bound and
   // the update's loads land on its critical path), so off by default.
@@ -1273,7 +1287,8 @@ class Batch final : public BatchIface {
 
   // The diffusion and copy kernels run on 8x32, 8x64 or 4x128 tiles.
   bool own_tile_list() const {
-    return strips || !((tile_r == 8 && (tile_c == 32 || tile_c == 64)) || (tile_r == 4 && tile_c == 128));
+    return strips || pair_rows ||
+           !((tile_r == 8 && (tile_c == 32 || tile_c == 64)) || (tile_r == 4 && tile_c == 128));
   }
   const WorkItem* tile_list() const { return own_tile_list() ? d_twl : d_wl; }
 
@@ -1365,28 +1380,31 @@ class Batch final : public BatchIface {
   }
 
   void append_items(int s, std::vector<WorkItem>& out, int& pcount) {
-    append_items_as(s, out, pcount, strips, tile_r, tile_c, true);
+    append_items_as(s, out, pcount, strips, tile_r, tile_c, true, pair_rows);
   }
 
   // Work items of member s: its whole-row tasks, then tiles (tr x tc) or
   // warp strips (bands of tr rows, kStripCols columns) over its runs of
   // ordinary rows.
   void append_items_as(int s, std::vector<WorkItem>& out, int& pcount, bool as_strips, int tr, int tc,
-                       bool own_partials) {
+                       bool own_partials, bool pairs = false) {
     const MemberRec& r = recs[s];
     const int N = r.N, M = r.M;
     int pbase = pcount;
     // Whole-row tasks first (they are the longest items).
     for (int j = 0; j < M; ++j)
       if (r.rowinfo[j] & RI_SPECIAL) {
+        // a task as two items (parts 0, 1) when split over a block pair
+        const int parts = pairs ? 2 : 1;
         if (split_rows) {
           // one task per field (no iap v on the north pole row): a row's
           // filters then run on three SMs
           for (int f : {F_GD, F_IU, F_IV})
-            if (f != F_IV || j < M - 1) out.push_back(WorkItem{s, 1, j, 0, 1, N, pcount++, f});
+            if (f != F_IV || j < M - 1)
+              for (int q = 0; q < parts; ++q) out.push_back(WorkItem{s, 1, j, q, parts, N, pcount++, f});
         } else {
           // one task for the three fields (the row is staged once)
-          out.push_back(WorkItem{s, 1, j, 0, 1, N, pcount++, -1});
+          for (int q = 0; q < parts; ++q) out.push_back(WorkItem{s, 1, j, q, parts, N, pcount++, -1});
         }
       }
     // Bulk tiles over runs of ordinary rows.
@@ -1432,6 +1450,14 @@ class Batch final : public BatchIface {
         ntiles += cols * ((recs[s].M + tile_r - 1) / tile_r);
       }
       split_rows = split_mode >= 0 ? split_mode == 1 : (sizeof(T) == 8 || ntiles < 8LL * num_sms);
+      long long nrows = 0;  // whole-row tasks
+      for (int s = 0; s < kSlots; ++s) {
+        if (!recs[s].used || !recs[s].active) continue;
+        for (int j = 0; j < recs[s].M; ++j) nrows += (recs[s].rowinfo[j] & RI_SPECIAL) ? (split_rows ? 3 : 1) : 0;
+      }
+      const bool can_pair = sizeof(T) == 8 && !strips && !weno() && !fuse_final;
+      pair_rows = can_pair && (pair_mode >= 0 ? pair_mode == 1
+                                              : (sizeof(T) == 8 && ntiles + nrows <= 2LL * num_sms));
     }
     for (int s = 0; s < kSlots; ++s) {
       if (!recs[s].used || !recs[s].active) continue;
@@ -1443,6 +1469,9 @@ class Batch final : public BatchIface {
     }
     hwl = rows_first;
     hwl.insert(hwl.end(), tiles.begin(), tiles.end());
+    // a paired launch runs clusters of two blocks: an even count (the pairs
+    // of a row task are consecutive from an even index: row tasks first)
+    if (pair_rows && hwl.size() % 2) hwl.push_back(WorkItem{active_slots.empty() ? 0 : active_slots[0], 3, 0, 0, 0, 0, -1, 0});
     nwork = (int)hwl.size();
     nrow = (int)rows_first.size();
     std::vector<WorkItem> htwl;
@@ -1539,6 +1568,7 @@ class Batch final : public BatchIface {
     a.ub_lat = P.uv_adv_upwind_lat_beta;
     a.rescale_rtol = P.filter_rescale_rtol;
     a.uvslot = d_uvslot;
+    a.pair = pair_rows ? 1 : 0;
     return a;
   }
 
@@ -1990,11 +2020,12 @@ int gdc_batch_diag(gdc_batch* b, int id, double* m, double* e, double* beta) {
 }
 int gdc_batch_active(gdc_batch* b, int* n) { return (b && n) ? b->impl->active(n) : GDC_E_CONFIG; }
 int gdc_batch_set_tile(gdc_batch* b, int r, int c) { return b ? b->impl->set_tile(r, c) : GDC_E_CONFIG; }
-int gdc_batch_set_schedule(gdc_batch* b, int split_rows, int fuse_final) {
-  return b ? b->impl->set_schedule(split_rows, fuse_final) : GDC_E_CONFIG;
+int gdc_batch_set_schedule(gdc_batch* b, int split_rows, int fuse_final, int pair_rows) {
+  return b ? b->impl->set_schedule(split_rows, fuse_final, pair_rows) : GDC_E_CONFIG;
 }
-int gdc_batch_get_schedule(gdc_batch* b, int* tile_rows, int* tile_cols, int* split_rows, int* fuse_final) {
-  return b ? b->impl->get_schedule(tile_rows, tile_cols, split_rows, fuse_final) : GDC_E_CONFIG;
+int gdc_batch_get_schedule(gdc_batch* b, int* tile_rows, int* tile_cols, int* split_rows, int* fuse_final,
+                           int* pair_rows) {
+  return b ? b->impl->get_schedule(tile_rows, tile_cols, split_rows, fuse_final, pair_rows) : GDC_E_CONFIG;
 }
 int gdc_batch_history(gdc_batch* b, int member_id, double* u_a, double* v_a, double* gh, double* div, double* vor,
                       int ld) {

@@ -201,10 +201,10 @@ enum Field { F_GD = 0, F_IU = 1, F_IV = 2 };
 
 struct WorkItem {
   int member;  // member slot
-  int kind;    // 0 bulk tile, 1 whole-row task
+  int kind;    // 0 bulk tile, 1 whole-row task, 3 nothing (padding)
   int j0;      // first row index (row task: the row)
-  int i0;      // first column (tile)
-  int rows;    // tile rows
+  int i0;      // first column (tile); row task: its part (0, 1) of a pair
+  int rows;    // tile rows; row task: 1, or 2 when split over a block pair
   int cols;    // tile columns
   int pidx;    // partial-sum slot
   int field;   // whole-row task: the one field it computes (F_GD, F_IU, F_IV), or -1 for all three
@@ -243,6 +243,10 @@ struct StageArgs {
   int fuse;
   int fin_base, fin_pass;
   double fin_h_scale;
+  // Launched as clusters of two blocks: a whole-row task listed as two
+  // items (WorkItem rows == 2, parts i0 = 0, 1 at an even and the next odd
+  // index) runs on the pair.
+  int pair;
 };
 
 // Warp strips: output columns per warp (lanes 1..30 of the 32), and the

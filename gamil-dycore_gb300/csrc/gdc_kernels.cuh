@@ -34,6 +34,8 @@
 #include <cmath>
 #include <cstdio>
 
+#include <cooperative_groups.h>
+
 #include "gdc_internal.h"
 
 namespace gdc {
@@ -724,14 +726,36 @@ struct Emit {
 // `tw` holds the member's twiddles in shared memory: cos(2 pi m/N) at
 // tw[m], sin at tw[N + m] (copied by twiddles_to_shared).  Indices k n mod
 // N advance by additions.
+//
+// A whole-row task split over the two blocks of a cluster (RowPair::on):
+// both blocks hold the whole row, each forms the coefficients of its parity
+// (p % 2 == part) and writes them to its own and its partner's shared
+// memory, and a cluster barrier before the writes (the partner has started
+// and is done with the previous filter's coefficients) and one after them
+// make all of them visible to both; each block then reconstructs the whole
+// row.  Every coefficient is the same sum as in one block.
+struct RowPair {
+  bool on = false;
+  int part = 0;
+};
+
 template <typename T>
-__device__ void filter_project(const MemberDev<T>& md, T* x, int keep, T* coefs, const T* tw) {
+__device__ void filter_project(const MemberDev<T>& md, T* x, int keep, T* coefs, const T* tw,
+                               RowPair pr = RowPair()) {
   const int N = md.N;
   const T* ctab = tw;
   const T* stab = tw + N;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  __syncthreads();
-  for (int p = warp; p < keep; p += nw) {
+  T* remote = nullptr;
+  if (pr.on) {
+    cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
+    cl.sync();
+    remote = cl.map_shared_rank(coefs, (int)cl.block_rank() ^ 1);
+  } else {
+    __syncthreads();
+  }
+  const int p0 = pr.on ? 2 * warp + pr.part : warp, dp = pr.on ? 2 * nw : nw;
+  for (int p = p0; p < keep; p += dp) {
     Acc<T> acc;
     if (p == 0) {
       for (int n = lane; n < N; n += 32) acc.add(x[n]);
@@ -747,9 +771,16 @@ __device__ void filter_project(const MemberDev<T>& md, T* x, int keep, T* coefs,
       }
     }
     warp_acc(acc);
-    if (lane == 0) coefs[p] = acc.value() * (p == 0 ? T(1.0) / T(N) : T(2.0) / T(N));
+    if (lane == 0) {
+      const T c = acc.value() * (p == 0 ? T(1.0) / T(N) : T(2.0) / T(N));
+      coefs[p] = c;
+      if (remote) remote[p] = c;
+    }
   }
-  __syncthreads();
+  if (pr.on)
+    cooperative_groups::this_cluster().sync();
+  else
+    __syncthreads();
   for (int n = threadIdx.x; n < N; n += blockDim.x) {
     T y = 0;
     y = y + coefs[0];
@@ -779,7 +810,7 @@ __device__ inline void twiddles_to_shared(const MemberDev<T>& md, T* tw) {
 // s1 or s2 is zero to within rtol of the sum of the magnitudes of its terms.
 template <typename T>
 __device__ void filter_rescale(const MemberDev<T>& md, T* x, const T* __restrict__ w1, const T* __restrict__ w2,
-                               int keep, T* coefs, T* red, double rtol, const T* tw) {
+                               int keep, T* coefs, T* red, double rtol, const T* tw, RowPair pr = RowPair()) {
   const int N = md.N;
   Acc<T> s, sa;
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
@@ -790,7 +821,7 @@ __device__ void filter_rescale(const MemberDev<T>& md, T* x, const T* __restrict
   const T s1 = block_value(s, red);
   const T a1 = rtol > 0 ? block_value(sa, red) : T(0);
   if (!(fabs(s1) > T(1.0e-16))) return;  // src/filter_mod.F90:31
-  filter_project(md, x, keep, coefs, tw);
+  filter_project(md, x, keep, coefs, tw, pr);
   Acc<T> q, qa;
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     const T t = x[i] * (w2 ? (w1[i] + w2[i]) : w1[i]);
@@ -1527,7 +1558,7 @@ __device__ __forceinline__ void strip_item(const MemberDev<T>& md, const WorkIte
 template <typename T, int PASS>
 __device__ void row_tail(const MemberDev<T>& md, const StageArgs& a, Emit<T>& em, int j, int f, T* x,
                          const Acc<double>& cap, T* coefs, T* redT, const T* gd_in, const T* iu_in,
-                         const T* iv_in, const T* tw) {
+                         const T* iv_in, const T* tw, RowPair pr) {
   const int N = md.N, M = md.M, Mh = md.Mh;
   const int info = md.rowinfo[j];
   const bool has_du = (j >= 1 && j <= M - 2);
@@ -1544,13 +1575,15 @@ __device__ void row_tail(const MemberDev<T>& md, const StageArgs& a, Emit<T>& em
   }
   const size_t ro = (size_t)j * N;
   if (f == F_IU && has_du && (info & RI_FLAG_FULL))
-    filter_rescale(md, x, iu_in + ro, (const T*)nullptr, ri_keep_full(info), coefs, redT, a.rescale_rtol, tw);
+    filter_rescale(md, x, iu_in + ro, (const T*)nullptr, ri_keep_full(info), coefs, redT, a.rescale_rtol, tw, pr);
   if (f == F_IV && (info & RI_FLAG_HALF))
-    filter_rescale(md, x, iv_in + ro, (const T*)nullptr, ri_keep_half(info), coefs, redT, a.rescale_rtol, tw);
+    filter_rescale(md, x, iv_in + ro, (const T*)nullptr, ri_keep_half(info), coefs, redT, a.rescale_rtol, tw, pr);
   if (f == F_GD && PASS != kSlowPass && (info & RI_FLAG_FULL))
-    filter_rescale(md, x, gd_in + ro, md.ghs + ro, ri_keep_full(info), coefs, redT, a.rescale_rtol, tw);
+    filter_rescale(md, x, gd_in + ro, md.ghs + ro, ri_keep_full(info), coefs, redT, a.rescale_rtol, tw, pr);
   const T w = f == F_IV ? ch(md, CH_COS, j) : cf(md, CF_COS, j);
-  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+  // a block of a pair updates its half of the row (num_lon is a multiple of 4)
+  const int i_end = pr.on ? (pr.part + 1) * (N / 2) : N;
+  for (int i = (pr.on ? pr.part * (N / 2) : 0) + threadIdx.x; i < i_end; i += blockDim.x) {
     const size_t o = ro + i;
     // du is 0 on pole rows (never assigned by the reference); inner
     // products skip pole-row du (src/types_mod.F90:355).
@@ -1569,9 +1602,37 @@ struct StageOcc {
 
 // One work item of a stage (a bulk tile or a whole-row task), by the block.
 template <typename T, int PASS, int ADV, int R, int W>
-__device__ __forceinline__ void stage_item(const MemberDev<T>* __restrict__ mems, const WorkItem w,
+__device__ __forceinline__ void stage_item(const MemberDev<T>* __restrict__ mems, const WorkItem* __restrict__ wl,
                                            const StageArgs& a, unsigned char* smem_raw, int staging_words,
                                            int max_n) {
+  const WorkItem w = wl[blockIdx.x];
+  if (w.kind > 1) return;  // padding of a paired launch to an even count
+  // A whole-row task split over a block pair (two consecutive items, parts
+  // 0 and 1, the pair's blocks of one cluster).  Both blocks decide alike
+  // (from the two items and the launch), so both or neither take the
+  // cluster barriers; an item whose partner is not there (a launch without
+  // clusters) is done whole by part 0, and part 1 contributes nothing.
+  RowPair pr;
+  if constexpr (sizeof(T) == 8) {  // FP64 only: FP32 launches have many items per SM
+  if (w.kind == 1 && w.rows == 2) {
+    bool paired = false;
+    if (a.pair && (int)cooperative_groups::this_cluster().num_blocks() == 2) {
+      const WorkItem q = wl[blockIdx.x ^ 1];
+      paired = q.kind == 1 && q.rows == 2 && q.member == w.member && q.j0 == w.j0 && q.field == w.field &&
+               q.i0 == (w.i0 ^ 1) && (int)(blockIdx.x & 1) == w.i0;
+    }
+    if (paired) {
+      pr.on = true;
+      pr.part = w.i0;
+    } else if (w.i0 == 1) {
+      if (a.do_ip && threadIdx.x == 0) {
+        double* pp = a.partials + 4 * (size_t)w.pidx;
+        pp[0] = pp[1] = pp[2] = pp[3] = 0.0;
+      }
+      return;
+    }
+  }
+  }
   T* staging = reinterpret_cast<T*>(smem_raw);  // bulk tile, or the row task's tile, then:
   T* rows = staging + row_task_words<T>();      // 3 * max_n (row tasks)
   T* coefs = rows + 3 * max_n;                  // kMaxKeep
@@ -1627,10 +1688,25 @@ __device__ __forceinline__ void stage_item(const MemberDev<T>* __restrict__ mems
     const bool want_u = f < 0 || f == F_IU, want_v = has_dv && (f < 0 || f == F_IV), want_g = f < 0 || f == F_GD;
     T* xr[3] = {rows + 2 * max_n, rows, rows + max_n};  // by field: gd, iap u, iap v
     if (f >= 0) xr[f] = rows;
+    // A pair splits the columns of a row without a pole cap: each block
+    // computes the raw tendencies of its columns (split at a multiple of 4,
+    // the staging copies' alignment) into its own and its partner's rows.
+    const bool split_cols = pr.on && !south && !north;
+    T* rx[3] = {nullptr, nullptr, nullptr};
+    int cb = 0, ce = N;
+    if (split_cols) {
+      cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
+      cl.sync();  // the partner has started
+      const int other = (int)cl.block_rank() ^ 1;
+      for (int q = 0; q < 3; ++q) rx[q] = cl.map_shared_rank(xr[q], other);
+      const int sp = (N / 2) & ~3;
+      cb = pr.part ? sp : 0;
+      ce = pr.part ? N : sp;
+    }
     Acc<double> cap;
     using TR = Tile<T, 1, kRowChunk>;
-    for (int c0 = 0; c0 < N; c0 += kRowChunk) {
-      const int vw = min(kRowChunk, N - c0);
+    for (int c0 = cb; c0 < ce; c0 += kRowChunk) {
+      const int vw = min(kRowChunk, ce - c0);
       TR t = carve<T, 1, kRowChunk>(staging, j, c0, 1, vw);
       __syncthreads();
       tile_issue(md, gd_in, iu_in, iv_in, t, given, PASS != kSlowPass, fuse ? md.td[TS_NEW] : nullptr);
@@ -1642,9 +1718,16 @@ __device__ __forceinline__ void stage_item(const MemberDev<T>* __restrict__ mems
         const int i = c0 + c;
         const TileView<T, TR> sv{t, p, j};
         const bool wl = ADV == GDC_ADV_WENO && PASS != kFastPass;
-        if (want_u)
-          xr[F_IU][i] = has_du ? point_du<T, PASS, ADV>(sv, ub_lon, ub_lat, wl ? md.wadv[0][j * N + i] : T(0)) : T(0);
-        if (want_v) xr[F_IV][i] = point_dv<T, PASS, ADV>(sv, ub_lon, ub_lat, wl ? md.wadv[1][j * N + i] : T(0));
+        if (want_u) {
+          const T x = has_du ? point_du<T, PASS, ADV>(sv, ub_lon, ub_lat, wl ? md.wadv[0][j * N + i] : T(0)) : T(0);
+          xr[F_IU][i] = x;
+          if (split_cols) rx[F_IU][i] = x;
+        }
+        if (want_v) {
+          const T x = point_dv<T, PASS, ADV>(sv, ub_lon, ub_lat, wl ? md.wadv[1][j * N + i] : T(0));
+          xr[F_IV][i] = x;
+          if (split_cols) rx[F_IV][i] = x;
+        }
         if (!want_g) continue;
         if (south || north) {
           // src/dycore_mod.F90:572-596: sp += (ig(j)+ig(j+1)) iv(j);
@@ -1657,20 +1740,25 @@ __device__ __forceinline__ void stage_item(const MemberDev<T>* __restrict__ mems
           }
           xr[F_GD][i] = T(0);
         } else {
-          xr[F_GD][i] = point_dgd<T, PASS>(sv);
+          const T x = point_dgd<T, PASS>(sv);
+          xr[F_GD][i] = x;
+          if (split_cols) rx[F_GD][i] = x;
         }
       }
     }
-    __syncthreads();
+    if (split_cols)
+      cooperative_groups::this_cluster().sync();  // both halves in both blocks' rows
+    else
+      __syncthreads();
     // The filter's weights are the input level: with a fused update, the
     // level this block has just formed and written for its own field(s) of
     // row j (visible to the block after the barrier above).
     const T* wg = fuse ? md.st[a.in_slot][F_GD] : gd_in;
     const T* wu = fuse ? md.st[a.in_slot][F_IU] : iu_in;
     const T* wv = fuse ? md.st[a.in_slot][F_IV] : iv_in;
-    if (want_u) row_tail<T, PASS>(md, a, em, j, F_IU, xr[F_IU], cap, coefs, redT, wg, wu, wv, tw);
-    if (want_v) row_tail<T, PASS>(md, a, em, j, F_IV, xr[F_IV], cap, coefs, redT, wg, wu, wv, tw);
-    if (want_g) row_tail<T, PASS>(md, a, em, j, F_GD, xr[F_GD], cap, coefs, redT, wg, wu, wv, tw);
+    if (want_u) row_tail<T, PASS>(md, a, em, j, F_IU, xr[F_IU], cap, coefs, redT, wg, wu, wv, tw, pr);
+    if (want_v) row_tail<T, PASS>(md, a, em, j, F_IV, xr[F_IV], cap, coefs, redT, wg, wu, wv, tw, pr);
+    if (want_g) row_tail<T, PASS>(md, a, em, j, F_GD, xr[F_GD], cap, coefs, redT, wg, wu, wv, tw, pr);
   }
 
   if (a.do_ip) {
@@ -1689,13 +1777,14 @@ __device__ __forceinline__ void stage_item(const MemberDev<T>* __restrict__ mems
   }
 }
 
-// A stage launch: one block per work item.
+// A stage launch: one block per work item (clusters of two blocks when
+// StageArgs::pair: then whole-row tasks may be split over a pair).
 template <typename T, int PASS, int ADV, int R, int W>
 __global__ void __launch_bounds__(kThreads, StageOcc<T>::kMinBlocks)
     stage_kernel(const MemberDev<T>* __restrict__ mems, const WorkItem* __restrict__ wl, StageArgs a,
                  int staging_words, int max_n) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  stage_item<T, PASS, ADV, R, W>(mems, wl[blockIdx.x], a, smem_raw, staging_words, max_n);
+  stage_item<T, PASS, ADV, R, W>(mems, wl, a, smem_raw, staging_words, max_n);
 }
 
 // Warp strips, one per warp (items cover every row of their members).
@@ -2347,7 +2436,24 @@ static int launch_stage_t(const MemberDev<T>* mem, const WorkItem* wl, int nwork
       return check_launch();
     configured.record(dev, smem);
   }
-  stage_kernel<T, PASS, ADV, R, W><<<nwork, kThreads, smem, s>>>(mem, wl, a, sw, max_n);
+  if (!a.pair) {
+    stage_kernel<T, PASS, ADV, R, W><<<nwork, kThreads, smem, s>>>(mem, wl, a, sw, max_n);
+    return check_launch();
+  }
+  if (nwork % 2) return GDC_E_CONFIG;  // clusters of two need an even count
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nwork);
+  cfg.blockDim = dim3(kThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = 2;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, stage_kernel<T, PASS, ADV, R, W>, mem, wl, a, sw, max_n);
   return check_launch();
 }
 

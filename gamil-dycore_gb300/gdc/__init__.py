@@ -153,8 +153,8 @@ def lib() -> ctypes.CDLL:
             "gdc_batch_diag": (ctypes.c_int, [vp, ctypes.c_int, dp, dp, dp]),
             "gdc_batch_active": (ctypes.c_int, [vp, ip]),
             "gdc_batch_set_tile": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
-            "gdc_batch_set_schedule": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
-            "gdc_batch_get_schedule": (ctypes.c_int, [vp, ip, ip, ip, ip]),
+            "gdc_batch_set_schedule": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+            "gdc_batch_get_schedule": (ctypes.c_int, [vp, ip, ip, ip, ip, ip]),
             "gdc_batch_checkpoint": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_char_p]),
             "gdc_batch_restore": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_size_t, ip]),
             "gdc_write_restart": (ctypes.c_int, [vp, ctypes.c_char_p]),
@@ -500,10 +500,12 @@ class Batch:
     def set_tile(self, rows: int, cols: int):
         self._check(lib().gdc_batch_set_tile(self.b, rows, cols))
 
-    def set_schedule(self, split_rows: int = -1, fuse_final: int = 1):
-        """Launch schedule: whole-row tasks split by field (-1 auto, 0, 1) and
-        the final update fused into the next stage (1) or launched (0)."""
-        self._check(lib().gdc_batch_set_schedule(self.b, split_rows, fuse_final))
+    def set_schedule(self, split_rows: int = -1, fuse_final: int = 0, pair_rows: int = -1):
+        """Launch schedule: whole-row tasks split by field (-1 auto, 0, 1),
+        the final update fused into the next stage (1) or launched (0), and
+        whole-row tasks split over the two blocks of a cluster (-1 auto, 0,
+        1)."""
+        self._check(lib().gdc_batch_set_schedule(self.b, split_rows, fuse_final, pair_rows))
 
     def autotune(self):
         """Time every launch schedule on the current members and keep the
@@ -515,9 +517,10 @@ class Batch:
 
     def schedule(self) -> dict:
         """The launch schedule in use: tile shape, row-task split, fusion."""
-        v = [ctypes.c_int() for _ in range(4)]
+        v = [ctypes.c_int() for _ in range(5)]
         self._check(lib().gdc_batch_get_schedule(self.b, *[ctypes.byref(x) for x in v]))
-        return {"tile": (v[0].value, v[1].value), "split_rows": v[2].value, "fuse_final": v[3].value}
+        return {"tile": (v[0].value, v[1].value), "split_rows": v[2].value, "fuse_final": v[3].value,
+                "pair_rows": v[4].value}
 
     def profile(self, nsteps: int):
         ms = (ctypes.c_double * 5)()

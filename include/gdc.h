@@ -324,18 +324,30 @@ int gdc_batch_active(gdc_batch* b, int* n_active);
  * whole choice. */
 int gdc_batch_set_tile(gdc_batch* b, int tile_rows, int tile_cols);
 /* Launch schedule of the stage kernels (a choice of how the work is
- * split, which gdc_batch_autotune also tunes): split_rows -1 picks
- * automatically (one task per field in FP64 and in batches with few tiles
- * per SM, one task per row otherwise), 0 one whole-row task per pole or
- * filtered row, 1 one task per field of such a row; fuse_final 1 (default)
- * forms each predict_correct's final update (src/dycore_mod.F90:789-790)
- * in the first stage of the next predict_correct of the same step instead
- * of a launch of its own (tiles only; WENO batches and warp strips always
- * launch it), 0 (default) launches it.  FP64 results are bitwise the same under every schedule;
- * FP32 results agree to rounding (the partial sums of beta group
- * differently). */
-int gdc_batch_set_schedule(gdc_batch* b, int split_rows, int fuse_final);
-int gdc_batch_get_schedule(gdc_batch* b, int* tile_rows, int* tile_cols, int* split_rows, int* fuse_final);
+ * split, which gdc_batch_autotune also tunes):
+ *   split_rows -1 picks automatically (one task per field in FP64 and in
+ *     batches with few tiles per SM, one task per row otherwise), 0 one
+ *     whole-row task per pole or filtered row, 1 one task per field of such
+ *     a row;
+ *   fuse_final 1 forms each predict_correct's final update
+ *     (src/dycore_mod.F90:789-790) in the first stage of the next
+ *     predict_correct of the same step instead of a launch of its own
+ *     (tiles only; WENO batches and warp strips always launch it), 0
+ *     (default) launches it;
+ *   pair_rows 1 runs the FP64 stage launches as clusters of two blocks
+ *     and splits each whole-row task over a pair (each block computes half
+ *     of the row's columns into both blocks, forms half of the filter's
+ *     coefficients and updates half of the row), 0 one block per task, -1
+ *     (default) automatically: FP64 launches with at most two work items
+ *     per SM (FP64 tiles only, not with fuse_final; FP32 batches never
+ *     pair).
+ * FP64 results are bitwise the same under every schedule; FP32 results
+ * agree to rounding (the partial sums of beta group differently).
+ * gdc_batch_get_schedule reports the tile shape and the schedule in effect
+ * (pair_rows: whether rows are split over pairs now). */
+int gdc_batch_set_schedule(gdc_batch* b, int split_rows, int fuse_final, int pair_rows);
+int gdc_batch_get_schedule(gdc_batch* b, int* tile_rows, int* tile_cols, int* split_rows, int* fuse_final,
+                           int* pair_rows);
 int gdc_batch_autotune(gdc_batch* b, int* tile_rows, int* tile_cols,
                        double* best_ms_per_step);
 

@@ -168,8 +168,9 @@ def test_warp_strips_other_schemes_match_oracle(native, split, adv):
 @pytest.mark.parametrize("split", [0, 1])
 def test_every_schedule_matches_oracle(native, split):
     """Whole-row or per-field row tasks, the final update launched or formed
-    by the next predict_correct's first stage: the FP64 path stays bitwise
-    the oracle's (csp2 with 6 subcycles: seven fused updates per step)."""
+    by the next predict_correct's first stage, row tasks on one block or
+    split over the two blocks of a cluster: the FP64 path stays bitwise the
+    oracle's (csp2 with 6 subcycles: seven fused updates per step)."""
     from oracle.oracle import OracleModel
     N, M = 360, 181
     p = scheme(gdc, N, M, 240.0)
@@ -178,16 +179,47 @@ def test_every_schedule_matches_oracle(native, split):
     o.set_state(*ic)
     o.step(3)
     ref = o.get_state()
-    for fuse in (0, 1):
+    for fuse, pair in ((0, 0), (1, 0), (0, 1)):
         b = gdc.Batch(p)
-        b.set_schedule(split, fuse)
+        b.set_schedule(split, fuse, pair)
         mid = b.add(N, M, 240.0, 3, *ic)
         b.step(3)
         b.sync()
-        assert b.schedule()["fuse_final"] == fuse
+        assert b.schedule()["fuse_final"] == fuse and b.schedule()["pair_rows"] == pair
         for name, a in zip(("u", "v", "gd"), b.get_state(mid)):
-            assert np.array_equal(interior(a), interior(ref[name])), (split, fuse, name)
+            assert np.array_equal(interior(a), interior(ref[name])), (split, fuse, pair, name)
         b.close()
+
+
+def test_paired_rows_in_a_mixed_batch(native):
+    """Row tasks split over block pairs in a mixed-grid FP64 batch (members
+    of different widths -- 180 columns split at 88, not at the middle --
+    whole-row and per-field tasks, pole rows) are bitwise the unpaired
+    batch's.  (The single-member FP64 model pairs its rows by default, and
+    its debug tendency -- a launch without clusters, where part 0 does a
+    paired task whole -- is checked against the oracle by the tendency
+    parity tests.)  FP32 batches never pair."""
+    grids = [(360, 181, 240.0), (180, 91, 480.0), (144, 73, 600.0)]
+    p = scheme(gdc, 360, 181, 240.0)
+    for split in (0, 1):
+        out = []
+        for pair in (0, 1):
+            b = gdc.Batch(p)
+            b.set_schedule(split, 0, pair)
+            ids = [b.add(N, M, dt, 4, *gdc.ic_seeded(N, M, seed=k)) for k, (N, M, dt) in enumerate(grids)]
+            b.step(4)
+            assert b.schedule()["pair_rows"] == pair
+            out.append([b.get_state(i) for i in ids])
+            b.close()
+        for s0, s1 in zip(*out):
+            for x, y in zip(s0, s1):
+                assert np.array_equal(x, y), split
+    b = gdc.Batch(scheme(gdc, 360, 181, 240.0, precision=gdc.FP32))
+    b.set_schedule(1, 0, 1)
+    b.add(180, 91, 480.0, 2, *gdc.ic_seeded(180, 91, seed=0))
+    b.step(2)
+    assert b.schedule()["pair_rows"] == 0
+    b.close()
 
 
 def test_fp32_fused_schedule_matches_launched(native):
@@ -233,7 +265,7 @@ def test_autotune_advances_no_forecast(native, prec):
     sch = a.schedule()
     if prec == gdc.FP32:
         b.set_tile(*sch["tile"])
-        b.set_schedule(sch["split_rows"], sch["fuse_final"])
+        b.set_schedule(sch["split_rows"], sch["fuse_final"], sch["pair_rows"])
     a.step(7)
     b.step(7)
     for i, j in zip(ia, ib):
