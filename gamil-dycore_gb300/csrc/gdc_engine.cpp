@@ -237,8 +237,11 @@ class Batch final : public BatchIface {
       for (int k = 0; k < 20; ++k) mp.zonal_tend_filter_cutoff_wavenumber[k] = cutoff[k];
     for (int k = 0; k < 20; ++k) {
       const int c = mp.zonal_tend_filter_cutoff_wavenumber[k];
-      if (c < 0 || 2 * (c + 1) >= N || 2 * (c + 1) > 120)
-        return fail(GDC_E_CONFIG, "zonal_tend_filter_cutoff_wavenumber out of range for this grid");
+      // the reference's factor rows hold 2 (c + 1) <= num_lon entries
+      // (src/filter_mod.F90:79-96 writes past the row beyond that)
+      if (c < 0 || 2 * (c + 1) > N)
+        return fail(GDC_E_CONFIG, "zonal_tend_filter_cutoff_wavenumber out of range for this grid "
+                                  "(0 <= c <= num_lon / 2 - 1)");
     }
     int slot = -1;
     for (int s = 0; s < kSlots; ++s)

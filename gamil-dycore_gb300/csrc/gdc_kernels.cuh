@@ -48,7 +48,6 @@ constexpr int kRowChunk = 128;  // columns per chunk of a whole-row task
 #ifndef GDC_STAGE_BLOCKS
 #define GDC_STAGE_BLOCKS 4  // resident stage blocks per SM the FP32 register budget targets
 #endif
-constexpr int kMaxKeep = 128;   // packed FFT coefficients a filter row may keep
 
 // ------------------------------------------------------------ helpers
 
@@ -772,7 +771,10 @@ __device__ void filter_project(const MemberDev<T>& md, T* x, int keep, T* coefs,
     }
     warp_acc(acc);
     if (lane == 0) {
-      const T c = acc.value() * (p == 0 ? T(1.0) / T(N) : T(2.0) / T(N));
+      // a0 and, when every mode is kept, the Nyquist term r(N) = (1/N)
+      // sum x (-1)^n (the cosine table is exactly +-1 there) take 1/N
+      const bool single = p == 0 || (p == N - 1 && N % 2 == 0);
+      const T c = acc.value() * (single ? T(1.0) / T(N) : T(2.0) / T(N));
       coefs[p] = c;
       if (remote) remote[p] = c;
     }
@@ -1635,8 +1637,8 @@ __device__ __forceinline__ void stage_item(const MemberDev<T>* __restrict__ mems
   }
   T* staging = reinterpret_cast<T*>(smem_raw);  // bulk tile, or the row task's tile, then:
   T* rows = staging + row_task_words<T>();      // 3 * max_n (row tasks)
-  T* coefs = rows + 3 * max_n;                  // kMaxKeep
-  T* tw = coefs + kMaxKeep;                     // 2 * max_n twiddles
+  T* coefs = rows + 3 * max_n;                  // max_n (a row keeps at most num_lon)
+  T* tw = coefs + max_n;                        // 2 * max_n twiddles
   T* redT = staging + staging_words;            // 64, then 64 doubles
   // The member descriptor is read in place (read-only, L1-cached): copying
   // it to shared memory cost a barrier per block.
@@ -2128,7 +2130,7 @@ __global__ void __launch_bounds__(kThreads)
   T* staging = reinterpret_cast<T*>(smem_raw);
   T* rows = staging + row_task_words<T>();
   T* coefs = rows + 3 * max_n;
-  T* tw = coefs + kMaxKeep;  // 2 * max_n twiddles
+  T* tw = coefs + max_n;  // 2 * max_n twiddles
   T* redT = staging + staging_words;
   double* redD = reinterpret_cast<double*>(redT + 64);
   __shared__ MemberDev<T> smd;
@@ -2416,7 +2418,7 @@ size_t stage_smem_bytes(int tile_rows, int tile_cols, int max_n, int* staging_wo
   // Rounded to 4 words and max_n to an even count so that the FP64
   // reduction buffer after the area stays 8-byte aligned.
   max_n = (max_n + 1) & ~1;
-  const int row = row_task_words<T>() + 3 * max_n + kMaxKeep + 2 * max_n;
+  const int row = row_task_words<T>() + 3 * max_n + max_n + 2 * max_n;
   const int sw = ((bulk > row ? bulk : row) + 3) & ~3;
   if (staging_words) *staging_words = sw;
   return (size_t)(sw + 64) * sizeof(T) + 64 * sizeof(double) + 16;

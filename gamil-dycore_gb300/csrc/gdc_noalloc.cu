@@ -73,7 +73,7 @@ extern "C" int gdc_tendency_noalloc(const gdc_params* p, int pass, const double*
                 "(scratch is 2 MiB)");
   for (int k = 0; k < 20; ++k) {
     const int c = p->zonal_tend_filter_cutoff_wavenumber[k];
-    if (c < 0 || 2 * (c + 1) >= N || 2 * (c + 1) > 120)
+    if (c < 0 || 2 * (c + 1) > N)
       return fail(GDC_E_CONFIG, "gdc_tendency_noalloc: zonal_tend_filter_cutoff_wavenumber out of range");
   }
   int dev = 0;

@@ -245,7 +245,9 @@ int gdc_device_mem_info(int device, size_t* free_bytes, size_t* total_bytes);
  * batched step at the next step boundary.  `cutoff` is the member's
  * zonal_tend_filter_cutoff_wavenumber (20 entries; NULL = the batch
  * scheme's): members of different resolutions filter different numbers of
- * polar rows.  GDC_E_OOM when free device memory minus `reserve_bytes`
+ * polar rows; each entry 0 <= c <= num_lon/2 - 1 (the reference's factor
+ * rows hold 2 (c+1) <= num_lon entries, src/filter_mod.F90:79-96), else
+ * GDC_E_CONFIG.  GDC_E_OOM when free device memory minus `reserve_bytes`
  * cannot hold it. */
 int gdc_batch_add(gdc_batch* b, int num_lon, int num_lat,
                   double time_step_size, long long nsteps, const int* cutoff,

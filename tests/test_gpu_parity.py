@@ -239,3 +239,32 @@ def test_iap_and_derived_state_read_back_bitwise(native):
     for a, name in ((iu, "iu"), (iv, "iv"), (ig, "ig"), (u, "u"), (v, "v"), (gd, "gd")):
         assert np.array_equal(interior(a), interior(s[name])), name
     m.close()
+
+
+def test_large_filter_cutoffs_match_oracle(native):
+    """Cutoffs up to num_lon/2 - 1 (the reference's factor rows hold 2 (c+1)
+    <= num_lon entries): every mode kept (c = 71 at 144 columns, with the
+    Nyquist coefficient), 61 and 35 kept pairs, and the usual 4 -- the
+    tendencies of every pass and 5 steps (rows split over block pairs by
+    default) are bitwise the oracle's; c = 72 is refused."""
+    N, M = 144, 73
+    cut = (71, 60, 35, 10, 4)
+    p = scheme(gdc, N, M, 600.0, cutoff=cut)
+    ic = gdc.ic_seeded(N, M, seed=4)
+    for pass_ in (0, 1, 2):
+        m, o = pair(p, ic)
+        for name, a, b in zip(("du", "dv", "dgd"), m.tendency(pass_), o.tendency(pass_)):
+            assert np.array_equal(interior(a), interior(b)), (pass_, name, rel_l2(a, b))
+        m.close()
+    m, o = pair(p, ic)
+    m.run(5)
+    o.step(5)
+    s = o.get_state()
+    for a, name in zip(m.get_state(), ("u", "v", "gd")):
+        assert np.array_equal(interior(a), interior(s[name])), name
+    assert m.diag() == o.diag()
+    m.close()
+    b = gdc.Batch(p)
+    with pytest.raises(gdc.GdcError):
+        b.add(N, M, 600.0, 1, *ic, cutoff=[72] + [4] * 4)
+    b.close()

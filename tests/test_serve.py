@@ -193,3 +193,10 @@ def test_nan_member_is_reported_and_counted_to_its_stop():
     assert st["completed"] == 3 and st["nan_members"] == 1
     assert st["nan_requests"] == [{"rid": 1, "grid": 180, "nsteps": 6, "nan_step": 2}]
     assert st["gpt_steps"] == reqs[0].points * (6 + 2 + 6)
+
+
+def test_fp32_serving_guards_the_rescale():
+    """FP32 serving skips the ill-conditioned s1/s2 rescale (guard 1e-5);
+    FP64 serving keeps the reference's rescale."""
+    assert serve.serving_scheme(gdc.FP32, 8).filter_rescale_rtol == pytest.approx(1e-5)
+    assert serve.serving_scheme(gdc.FP64, 8).filter_rescale_rtol == 0.0
