@@ -268,3 +268,21 @@ def test_large_filter_cutoffs_match_oracle(native):
     with pytest.raises(gdc.GdcError):
         b.add(N, M, 600.0, 1, *ic, cutoff=[72] + [4] * 4)
     b.close()
+
+
+@pytest.mark.parametrize("grid", [(16, 11), (20, 9)])
+def test_tiny_grids_match_oracle(native, grid):
+    """Grids smaller than one tile (16 or 20 columns: one partial tile per
+    row band, the wrap seam inside it) with two filtered rows per pole:
+    10 csp2 steps bitwise the oracle's."""
+    N, M = grid
+    p = scheme(gdc, N, M, 1800.0, cutoff=(2, 1))
+    ic = gdc.ic_seeded(N, M, seed=9, lmax=2)
+    m, o = pair(p, ic)
+    m.run(10)
+    o.step(10)
+    s = o.get_state()
+    for a, name in zip(m.get_state(), ("u", "v", "gd")):
+        assert np.array_equal(interior(a), interior(s[name])), (name, rel_l2(a, s[name]))
+    assert m.diag() == o.diag()
+    m.close()
