@@ -585,6 +585,10 @@ def run_ours(args, rank, world, dist):
     value, ms_all = replica_value(dist, gpt, ms)
     plain = plain_fp64(gdc, torch, ts)
     precision = precision_config1(gdc, torch, ts)
+    # one untimed job first (as the warm-up steps of the device-side figure:
+    # first-use costs of the process -- page-locked staging, the host pool,
+    # the allocator -- are not per-job costs), then the timed job
+    e2e_batch(gdc, torch, members, min(args.steps, 2), gdc.FP32, sched)
     e2e_ms, e2e_gpt, h2d, d2h = e2e_batch(gdc, torch, members, args.steps, gdc.FP32, sched)
     e2e_ms = reduce_max(dist, e2e_ms)
     prof_ms, prof_n = profile_kernels(gdc, members, gdc.FP32, sched=sched)

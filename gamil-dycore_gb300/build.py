@@ -89,13 +89,13 @@ def build(force: bool = False, verbose: bool = False) -> Path:
             # No FMA contraction in host code: the mesh and coefficient tables
             # round exactly as the reference's (and the same on x86 and Arm,
             # where g++ contracts by default).
-            cmds.append(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-Wall",
+            cmds.append(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-Wall", "-pthread",
                          f"-I{cuda / 'include'}", f"-I{INCLUDE}", "-c", str(src), "-o", str(obj)])
         if verbose:
             for c in cmds:
                 print(" ".join(c))
         _run_all(cmds)
-        link = [nvcc, *ARCH, "-shared", "-o", str(lib), *map(str, objs), "-lcudart"]
+        link = [nvcc, *ARCH, "-shared", "-o", str(lib), *map(str, objs), "-lcudart", "-lpthread"]
         _run_all([link])
     drv_src = CSRC / "dycore_test.cpp"
     drv = OUT / "dycore_test"

@@ -15,8 +15,12 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <condition_variable>
+#include <functional>
 #include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <type_traits>
 #include <vector>
 
@@ -114,6 +118,78 @@ struct PinnedStage {
   ~PinnedStage() {
     if (pinned && p) cudaFreeHost(p);
   }
+};
+
+// Host threads for the padded copies between the staging buffers and the
+// caller's arrays (one core copies at a fraction of the host's memory
+// bandwidth; a read-back of a 720x361 member is 6 MB).  One process-wide
+// pool, started on first use; one parallel_for at a time, the caller taking
+// items too.
+class HostPool {
+ public:
+  static HostPool& get() {
+    static HostPool pool;
+    return pool;
+  }
+  // f(i) for i in [0, n); returns when every call has returned.
+  void parallel_for(int n, const std::function<void(int)>& f) {
+    if (n <= 0) return;
+    if (workers_.empty() || n == 1) {
+      for (int i = 0; i < n; ++i) f(i);
+      return;
+    }
+    std::lock_guard<std::mutex> one(call_);
+    std::unique_lock<std::mutex> g(m_);
+    f_ = &f;
+    n_ = n;
+    next_ = 0;
+    left_ = n;
+    cv_.notify_all();
+    while (next_ < n_) {
+      const int i = next_++;
+      g.unlock();
+      f(i);
+      g.lock();
+      --left_;
+    }
+    done_.wait(g, [&] { return left_ == 0; });
+    f_ = nullptr;
+    n_ = next_ = 0;
+  }
+  ~HostPool() {
+    {
+      std::lock_guard<std::mutex> g(m_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for (auto& t : workers_) t.join();
+  }
+
+ private:
+  HostPool() {
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int n = (int)std::min(hw > 1 ? hw - 1 : 0u, 7u);
+    for (int k = 0; k < n; ++k) workers_.emplace_back([this] { loop(); });
+  }
+  void loop() {
+    std::unique_lock<std::mutex> g(m_);
+    for (;;) {
+      cv_.wait(g, [&] { return stop_ || next_ < n_; });
+      if (stop_) return;
+      const int i = next_++;
+      const std::function<void(int)>* f = f_;
+      g.unlock();
+      (*f)(i);
+      g.lock();
+      if (--left_ == 0) done_.notify_all();
+    }
+  }
+  std::vector<std::thread> workers_;
+  std::mutex call_, m_;
+  std::condition_variable cv_, done_;
+  const std::function<void(int)>* f_ = nullptr;
+  int n_ = 0, next_ = 0, left_ = 0;
+  bool stop_ = false;
 };
 
 struct MemberRec {
@@ -842,13 +918,36 @@ class Batch final : public BatchIface {
     // Each element of the padded array written once: zero latitude-halo
     // rows, then per interior row its values, periodic longitude halo and
     // zero padding past N + 4.
-    auto put = [&](double* f, int rows, const double* src) {
-      if (!f) return;
-      std::memset(f, 0, sizeof(double) * (size_t)ld * 2);
-      std::memset(f + (size_t)(rows + 2) * ld, 0, sizeof(double) * (size_t)ld * 2);
-      for (int j = 0; j < rows; ++j) {
-        double* row = f + (size_t)(j + 2) * ld;
-        const double* sr = src + (size_t)j * N;
+    // Bands of kBand rows of each requested field, over the host pool.
+    constexpr int kBand = 16;
+    struct Put {
+      double* f;
+      int rows;
+      const double* src;
+    };
+    std::vector<Put> puts;
+    auto want = [&](double* f, int rows, const double* src) {
+      if (f) puts.push_back(Put{f, rows, src});
+    };
+    want(gd, M, hg);
+    want(iu, M, hu);
+    want(iv, Mh, hv);
+    want(ig, M, sg);
+    if (!ic_uv && uv_mode != 2) {
+      want(u, M, ou);
+      want(v, Mh, ov);
+    }
+    std::vector<std::pair<int, int>> bands;  // (put, first row)
+    for (int k = 0; k < (int)puts.size(); ++k)
+      for (int j = 0; j < puts[k].rows; j += kBand) bands.push_back({k, j});
+    HostPool::get().parallel_for((int)bands.size(), [&](int b) {
+      const Put& q = puts[bands[b].first];
+      const int j0 = bands[b].second, j1 = std::min(q.rows, j0 + kBand);
+      if (j0 == 0) std::memset(q.f, 0, sizeof(double) * (size_t)ld * 2);
+      if (j1 == q.rows) std::memset(q.f + (size_t)(q.rows + 2) * ld, 0, sizeof(double) * (size_t)ld * 2);
+      for (int j = j0; j < j1; ++j) {
+        double* row = q.f + (size_t)(j + 2) * ld;
+        const double* sr = q.src + (size_t)j * N;
         std::memcpy(row + 2, sr, N * sizeof(double));
         row[0] = sr[N - 2];
         row[1] = sr[N - 1];
@@ -856,11 +955,7 @@ class Batch final : public BatchIface {
         row[N + 3] = sr[1];
         if (ld > N + 4) std::memset(row + N + 4, 0, sizeof(double) * (ld - N - 4));
       }
-    };
-    put(gd, M, hg);
-    put(iu, M, hu);
-    put(iv, Mh, hv);
-    put(ig, M, sg);
+    });
     if (ic_uv) {
       // state(old) still holds the initial condition's own u and v.
       auto copy_ic = [&](double* f, const std::vector<double>& src, int rows) {
@@ -870,9 +965,6 @@ class Batch final : public BatchIface {
       };
       copy_ic(u, r.ic_u, M);
       copy_ic(v, r.ic_v, Mh);
-    } else if (uv_mode != 2) {
-      put(u, M, ou);
-      put(v, Mh, ov);
     }
     return GDC_OK;
   }
