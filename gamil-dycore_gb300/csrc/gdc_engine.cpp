@@ -529,12 +529,20 @@ class Batch final : public BatchIface {
       }
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_uvslot + slot, &lvl, sizeof(int), cudaMemcpyHostToDevice, stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) {
+      cudaStreamSynchronize(stream);
       release(slot);
       return fail(GDC_E_CUDA, cuda_msg("add: upload", e));
     }
-    return finish(slot, id);
+    // The initial diagnostics follow in the same stream and end with its
+    // synchronisation: the caller's arrays (read in place) and the staging
+    // areas are free when this returns.
+    if (int rc = finish(slot, id)) {
+      cudaStreamSynchronize(stream);
+      release(slot);
+      return rc;
+    }
+    return GDC_OK;
   }
 
   // A member whose initial condition is generated in device memory
@@ -1312,6 +1320,7 @@ class Batch final : public BatchIface {
   size_t ictmp_cap = 0;       // its capacity in doubles
   PinnedStage stage_ic;       // host staging of the same
   PinnedStage stage_tab;      // host staging of an admitted member's tables
+  PinnedStage stage_diag;     // host staging of its initial diagnostics' items
   // the initial diagnostics' work items, partials and member slot
   FlatItem* d_idl = nullptr;
   double* d_ipart = nullptr;
@@ -1932,10 +1941,11 @@ class Batch final : public BatchIface {
       return fail(GDC_E_OOM, "initial diag: cudaMalloc");
     }
     // the items, the slot and the descriptor (its diag fields changed) from
-    // the table staging area, after the member's upload in the stream
+    // a staging area of their own (the member's table upload from stage_tab
+    // may still be in the stream; this call ends with the stream's
+    // synchronisation)
     const size_t bytes = sizeof(FlatItem) * wl.size();
-    sync_stream();  // the member's table upload has left the staging area
-    char* st = stage_tab.get(bytes + sizeof(MemberDev<T>) + 16);
+    char* st = stage_diag.get(bytes + sizeof(MemberDev<T>) + 16);
     std::memcpy(st, wl.data(), bytes);
     std::memcpy(st + bytes, &hdesc[slot], sizeof(MemberDev<T>));
     std::memcpy(st + bytes + sizeof(MemberDev<T>), &slot, sizeof(int));
