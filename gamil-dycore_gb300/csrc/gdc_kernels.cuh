@@ -1823,17 +1823,49 @@ __global__ void __launch_bounds__(kThreads, StripOcc<T>::kMinBlocks)
 // 784-787; isp :743-747), reduced by the whole block in a fixed order.
 // FP64: double-double (the oracle's correctly rounded sums); FP32: the
 // partials carry FP32 rounding, a plain FP64 sum loses nothing.
-template <typename T>
-__device__ void member_beta(const MemberDev<T>& md, int s, const double* partials, double* beta, int qcon,
-                            int beta_mode, double* red) {
-  typename DiagAcc<T>::type a1, a2;
-  for (int q = threadIdx.x; q < md.pcount; q += blockDim.x) {
-    const double* pp = partials + 4 * (size_t)(md.pbase + q);
+// The two sums over a member's partial slots (4 doubles each: two
+// accumulators as value and compensation) by one warp.  A member has one
+// slot per work item -- tens to a few hundred -- and in FP64 every further
+// warp's share of the merge tree is FP64 work on the SM's narrow FP64 pipe.
+template <typename A>
+__device__ void warp_partials(const double* partials, int base, int count, A& a1, A& a2) {
+  for (int q = threadIdx.x & 31; q < count; q += 32) {
+    const double* pp = partials + 4 * (size_t)(base + q);
     a1.merge(pp[0], pp[1]);
     a2.merge(pp[2], pp[3]);
   }
-  const double ip1 = block_value(a1, red);
-  const double ip2 = block_value(a2, red);
+  warp_acc(a1);
+  warp_acc(a2);
+}
+
+// The partial sums of a member: one warp in FP64 (double-double merges on
+// the narrow FP64 pipe), the whole block in FP32 (plain FP64 merges: the
+// latency of a longer serial merge per lane is what counts there).
+template <typename T, typename A>
+__device__ void member_partials(const double* partials, int base, int count, A& a1, A& a2) {
+  if constexpr (sizeof(T) == 8) {
+    warp_partials(partials, base, count, a1, a2);
+  } else {
+    __shared__ double red[64];
+    for (int q = threadIdx.x; q < count; q += blockDim.x) {
+      const double* pp = partials + 4 * (size_t)(base + q);
+      a1.merge(pp[0], pp[1]);
+      a2.merge(pp[2], pp[3]);
+    }
+    a1 = block_acc(a1, red);
+    a2 = block_acc(a2, red);
+  }
+}
+// Threads of a beta or diag_finalize block.
+template <typename T>
+constexpr int partial_threads() { return sizeof(T) == 8 ? 32 : kThreads; }
+
+template <typename T>
+__device__ void member_beta(const MemberDev<T>& md, int s, const double* partials, double* beta, int qcon,
+                            int beta_mode) {
+  typename DiagAcc<T>::type a1, a2;
+  member_partials<T>(partials, md.pbase, md.pcount, a1, a2);
+  const double ip1 = a1.value(), ip2 = a2.value();
   if (threadIdx.x == 0) {
     double b;
     if (sizeof(T) == 4 && beta_mode == 0) {
@@ -1852,9 +1884,8 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads)
     beta_kernel(const MemberDev<T>* __restrict__ mems, const int* __restrict__ slots, const double* partials,
                 double* beta, int qcon, int beta_mode) {
-  __shared__ double red[64];
   const int s = slots[blockIdx.x];
-  member_beta<T>(mems[s], s, partials, beta, qcon, beta_mode, red);
+  member_beta<T>(mems[s], s, partials, beta, qcon, beta_mode);
 }
 
 // ------------------------------------------------------ final update
@@ -2057,17 +2088,11 @@ __global__ void __launch_bounds__(kThreads)
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
     diag_finalize_kernel(const MemberDev<T>* __restrict__ mems, const int* __restrict__ slots, DiagArgs a) {
-  __shared__ double red[64];
   const int s = slots[blockIdx.x];
   const MemberDev<T>& md = mems[s];
   Acc<double> m, e;
-  for (int q = threadIdx.x; q < md.dcount; q += blockDim.x) {
-    const double* pp = a.partials + 4 * (size_t)(md.dbase + q);
-    m.merge(pp[0], pp[1]);
-    e.merge(pp[2], pp[3]);
-  }
-  const double tm = block_value(m, red);
-  const double te = block_value(e, red);
+  member_partials<T>(a.partials, md.dbase, md.dcount, m, e);
+  const double tm = m.value(), te = e.value();
   if (threadIdx.x == 0) {
     const double total_mass = tm * (kRadius * kRadius);
     a.diag[3 * s] = total_mass;
@@ -2651,7 +2676,8 @@ template <typename T>
 int launch_beta(const MemberDev<T>* mem, const int* slots, int nmembers, const double* partials, double* beta,
                 int qcon, int beta_mode, void* stream) {
   if (nmembers <= 0) return GDC_OK;
-  beta_kernel<T><<<nmembers, kThreads, 0, (cudaStream_t)stream>>>(mem, slots, partials, beta, qcon, beta_mode);
+  beta_kernel<T><<<nmembers, partial_threads<T>(), 0, (cudaStream_t)stream>>>(mem, slots, partials, beta, qcon,
+                                                                             beta_mode);
   return check_launch();
 }
 
@@ -2669,7 +2695,7 @@ int launch_diag(const MemberDev<T>* mem, const FlatItem* dl, int ndl, const int*
   diag_kernel<T><<<ndl, kThreads, 0, (cudaStream_t)stream>>>(mem, dl, a);
   int rc = check_launch();
   if (rc) return rc;
-  diag_finalize_kernel<T><<<nmembers, kThreads, 0, (cudaStream_t)stream>>>(mem, slots, a);
+  diag_finalize_kernel<T><<<nmembers, partial_threads<T>(), 0, (cudaStream_t)stream>>>(mem, slots, a);
   return check_launch();
 }
 
