@@ -1475,11 +1475,11 @@ class Batch final : public BatchIface {
     return e;
   }
 
-  // Diag items of member s: bands of kDiagRows rows.
+  // Diag items of member s: bands of diag_rows<T>() rows.
   void append_diag_items(int s, std::vector<FlatItem>& out) {
     hdesc[s].dbase = (int)out.size();
-    for (int j = 0; j < recs[s].M; j += kDiagRows)
-      out.push_back(FlatItem{s, 0, j, std::min(kDiagRows, recs[s].M - j)});
+    constexpr int R = diag_rows<T>();
+    for (int j = 0; j < recs[s].M; j += R) out.push_back(FlatItem{s, 0, j, std::min(R, recs[s].M - j)});
     hdesc[s].dcount = (int)out.size() - hdesc[s].dbase;
   }
 

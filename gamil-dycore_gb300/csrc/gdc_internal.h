@@ -324,8 +324,11 @@ int launch_final(const MemberDev<T>* mem, const FlatItem* fl, int nflat, const F
 template <typename T>
 int launch_diag(const MemberDev<T>* mem, const FlatItem* dl, int ndl, const int* slots,
                 int nmembers, const DiagArgs& a, void* stream);
-// Rows per diag item (one warp per row).
-constexpr int kDiagRows = 8;
+// Rows per diag item (one warp per row): 8 in FP32; 2 in FP64, whose row
+// sums are double-double FP64 work -- few rows per block spread it over
+// more SMs' FP64 pipes.
+template <typename T>
+constexpr int diag_rows() { return sizeof(T) == 8 ? 2 : 8; }
 // beta of each member in `slots` from the stage kernel's partials.
 template <typename T>
 int launch_beta(const MemberDev<T>* mem, const int* slots, int nmembers, const double* partials,

@@ -2692,7 +2692,7 @@ template <typename T>
 int launch_diag(const MemberDev<T>* mem, const FlatItem* dl, int ndl, const int* slots, int nmembers,
                 const DiagArgs& a, void* stream) {
   if (ndl <= 0) return GDC_OK;
-  diag_kernel<T><<<ndl, kThreads, 0, (cudaStream_t)stream>>>(mem, dl, a);
+  diag_kernel<T><<<ndl, 32 * diag_rows<T>(), 0, (cudaStream_t)stream>>>(mem, dl, a);
   int rc = check_launch();
   if (rc) return rc;
   diag_finalize_kernel<T><<<nmembers, partial_threads<T>(), 0, (cudaStream_t)stream>>>(mem, slots, a);
