@@ -103,7 +103,7 @@ int main(int argc, char** argv) {
       rc = gdc_ic_shallow_water_waves(N, M, u.data(), v.data(), gd.data(), ghs.data(), ld);
     else if (tc == "jet_zonal_flow") {
       gdc_destroy(h);
-      return fail("dycore_test", "jet_zonal_flow needs QUADPACK's integrals, which this build does not provide");
+      return fail("dycore_test", "jet_zonal_flow needs QUADPACK's integrals, which this library does not provide");
     } else {
       gdc_destroy(h);
       std::printf(" [Error]: Unknown test case %s!\n", tc.c_str());

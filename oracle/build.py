@@ -4,14 +4,14 @@ Compiles gdc_oracle.c and gdc_fftpack.c with gcc into oracle/_build/ at -O2
 with FMA contraction and fast-math disabled, so that the C evaluation order
 is the order written in the source (which follows the reference's):
 
-* libgdc_oracle.so -- the checker: correctly rounded sums, the filter as a
+* libgdc_oracle.so -- the exact build: correctly rounded sums, the filter as a
   projection onto the kept modes (the CUDA path's arithmetic);
 * libgdc_oracle_ref.so -- the reference's order: plain running sums in the
   reference's loop order (-DGDO_PLAIN_SUMS); with gdo_set_fft the filter
   runs FFTPACK's transforms as the reference does;
 * libgdc_oracle_fast.so -- the same reference-order arithmetic compiled
   with the reference's own flags (-Ofast, CMakeLists.txt:13): the timed CPU
-  baseline, never a checker.
+  baseline, never used to check.
 
 The reference (Fortran 2003) itself cannot be compiled here: no Fortran
 compiler exists on either machine, and its datetime/container submodules

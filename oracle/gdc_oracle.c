@@ -1,6 +1,6 @@
 /*
  * gdc_oracle.c -- CPU restatement (FP64, single thread) of the gamil-dycore
- * barotropic time step.  TEST INFRASTRUCTURE ONLY: the parity checker for
+ * barotropic time step.  TEST INFRASTRUCTURE ONLY: the parity reference for
  * the CUDA path and the timed CPU baseline.  Nothing in the product links it.
  *
  * Parity status: unpinned by reference outputs (the Fortran reference cannot

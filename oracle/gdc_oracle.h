@@ -4,7 +4,7 @@
  * TEST INFRASTRUCTURE ONLY.  This is the parity oracle: a plain-C, FP64,
  * single-threaded restatement of the reference's hot path, used by tests/,
  * by __graft_entry__.smoke() and by bench.py's cpu_baseline / reference arm
- * as the checker.  The product library never links, loads or calls it.
+ * to check the CUDA path.  The product library never links, loads or calls it.
  *
  * Parity status: unpinned by reference outputs.  The reference (Fortran 2003)
  * cannot be compiled in this environment (no Fortran compiler, empty

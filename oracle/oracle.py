@@ -1,7 +1,7 @@
 """ctypes wrapper of the CPU oracle (test infrastructure only).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs use
-this module, as the checker; the product never imports it.  Arrays use the
+this module, to check the CUDA path; the product never imports it.  Arrays use the
 reference's padded layout, numpy shape (rows + 4, num_lon + 4).
 """
 from __future__ import annotations
@@ -18,11 +18,11 @@ _P = ctypes.POINTER(ctypes.c_double)
 
 
 def lib(kind: str = "exact") -> ctypes.CDLL:
-    """One build of the oracle: "exact" (the checker: correctly rounded sums,
+    """One build of the oracle: "exact" (correctly rounded sums,
     the filter as a projection -- the CUDA path's arithmetic), "ref" (the
     reference's order: plain running sums in its loop order; FFTPACK's
     transforms with fft=True) or "fast" (the reference-order arithmetic at
-    -Ofast: the timed CPU baseline, never a checker)."""
+    -Ofast: the timed CPU baseline, never used to check)."""
     if kind is True:
         kind = "fast"
     elif kind is False:

@@ -1,7 +1,7 @@
 """The plain FP64 path against the reference's own order of arithmetic, and
 on the reference's own namelists.
 
-The CUDA path is bitwise equal to the checker oracle, whose reductions are
+The CUDA path is bitwise equal to the exact-sum oracle, whose reductions are
 correctly rounded sums and whose polar filter is a projection onto the
 kept modes (test_gpu_parity).  The reference instead adds with running sums
 in its loop order (src/dycore_mod.F90:212-216, 576-591,
@@ -90,7 +90,7 @@ def test_reference_namelist_one_day(native, name, make_ic):
     0.1, 8 subcycles, cutoffs 4,4,4) and rh_test (360x180, 10 subcycles,
     cutoffs 4 x 5) read through the namelist reader and run for one model
     day from the reference's own initial conditions: bitwise equal to the
-    checker oracle (state, mass, energy, beta), and within rounding of the
+    exact-sum oracle (state, mass, energy, beta), and within rounding of the
     reference-order oracle."""
     p, _, _ = gdc.read_namelist(GOLDEN / name)
     assert p.num_lat % 2 == 0

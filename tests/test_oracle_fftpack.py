@@ -1,6 +1,6 @@
 """The oracle's reference-order arithmetic (no GPU).
 
-The checker oracle evaluates every reduction as a correctly rounded sum and
+The exact-sum oracle evaluates every reduction as a correctly rounded sum and
 the polar filter as a projection onto the kept modes; the reference-order
 build instead keeps the reference's running sums in its loop order and runs
 the filter through FFTPACK 5.1's transforms (lib/fft/rfftf1.f, rfftb1.f and
