@@ -1188,21 +1188,32 @@ __device__ __forceinline__ void bulk_tile_pair(const MemberDev<float>& md, const
     if (UF == UF_PREDICT_OUT || UF == UF_CORRECT) tdst[f] = md.td[a.tout][f];
   }
   const F2 h(em.h);
+  // All of the thread's tendencies first, then its stores: the stencil
+  // values its rows share are loaded from shared memory once (a global
+  // store between them would make the compiler load them again).
+  F2 tdu[RPT], tdv[RPT], tdg[RPT];
+#pragma unroll
+  for (int k = 0; k < RPT; ++k) {
+    const int r = r0 + k;
+    const int j = w.j0 + r, o = ob + k * N;
+    const int p = TL::pos(r + 1, c + 1);
+    const TileView2<TL> sv{t, p, j};
+    F2 wu(0.0f), wv(0.0f);
+    if (ADV == GDC_ADV_WENO && PASS != kFastPass && cval && r < w.rows) {
+      wu = ld2(md.wadv[0] + o);
+      wv = ld2(md.wadv[1] + o);
+    }
+    tdu[k] = point_du<F2, PASS, ADV>(sv, F2(ub_lon), F2(ub_lat), wu);
+    tdv[k] = point_dv<F2, PASS, ADV>(sv, F2(ub_lon), F2(ub_lat), wv);
+    tdg[k] = point_dgd<F2, PASS>(sv);
+  }
 #pragma unroll
   for (int k = 0; k < RPT; ++k) {
     const int r = r0 + k;
     if (!cval || r >= w.rows) continue;
     const int j = w.j0 + r, o = ob + k * N;
     const int p = TL::pos(r + 1, c + 1);
-    const TileView2<TL> sv{t, p, j};
-    F2 wu(0.0f), wv(0.0f);
-    if (ADV == GDC_ADV_WENO && PASS != kFastPass) {
-      wu = ld2(md.wadv[0] + o);
-      wv = ld2(md.wadv[1] + o);
-    }
-    const F2 du = point_du<F2, PASS, ADV>(sv, F2(ub_lon), F2(ub_lat), wu);
-    const F2 dv = point_dv<F2, PASS, ADV>(sv, F2(ub_lon), F2(ub_lat), wv);
-    const F2 dg = point_dgd<F2, PASS>(sv);
+    const F2 du = tdu[k], dv = tdv[k], dg = tdg[k];
     if (UF == UF_PREDICT_IN) {
       st2(dst[F_IU] + o, ld2(t.iu + p) + h * du);
       st2(dst[F_IV] + o, ld2(t.iv + p) + h * dv);
