@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstring>
 #include <condition_variable>
+#include <cstdint>
 #include <functional>
 #include <memory>
 #include <mutex>
@@ -192,6 +193,44 @@ class HostPool {
   bool stop_ = false;
 };
 
+// Member state lives in the device's stream-ordered memory pool: a member's
+// memory is taken and given back in its batch's stream (no device-wide
+// synchronisation, as cudaFree makes), and freed memory stays reserved in
+// the pool for the next admission instead of going back to the driver.
+// The pool's reserve that is not in use counts as free device memory.
+cudaMemPool_t member_pool(int device) {
+  static std::mutex m;
+  static std::vector<cudaMemPool_t> pools;
+  std::lock_guard<std::mutex> g(m);
+  if ((int)pools.size() <= device) pools.resize(device + 1, nullptr);
+  if (!pools[device]) {
+    cudaMemPool_t p = nullptr;
+    if (cudaDeviceGetDefaultMemPool(&p, device) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+    pools[device] = p;
+  }
+  return pools[device];
+}
+
+// Free device memory for admission: the driver's free memory plus the
+// member pool's reserve not in use.
+size_t free_device_memory(int device) {
+  size_t f = 0, t = 0;
+  cudaMemGetInfo(&f, &t);
+  if (cudaMemPool_t p = member_pool(device)) {
+    uint64_t reserved = 0, used = 0;
+    if (cudaMemPoolGetAttribute(p, cudaMemPoolAttrReservedMemCurrent, &reserved) == cudaSuccess &&
+        cudaMemPoolGetAttribute(p, cudaMemPoolAttrUsedMemCurrent, &used) == cudaSuccess && reserved > used)
+      f += (size_t)(reserved - used);
+  }
+  cudaGetLastError();
+  return f;
+}
+
 struct MemberRec {
   bool used = false, active = false, finished = false, nan = false;
   int N = 0, M = 0;
@@ -327,12 +366,11 @@ class Batch final : public BatchIface {
       }
     if (slot < 0) return fail(GDC_E_OOM, "add: member table full");
     const Layout L = make_layout<T>(mp, N, M);
-    size_t free_b = 0, total_b = 0;
-    cudaMemGetInfo(&free_b, &total_b);
+    const size_t free_b = free_device_memory(P.device);
     if (free_b < L.total + reserve + extra) return fail(GDC_E_OOM, "add: not enough free device memory");
     MemberRec& r = recs[slot];
     r = MemberRec();
-    cudaError_t e = cudaMalloc(&r.dmem, L.total);
+    cudaError_t e = member_pool(P.device) ? cudaMallocAsync(&r.dmem, L.total, stream) : cudaMalloc(&r.dmem, L.total);
     if (e != cudaSuccess) {
       cudaGetLastError();
       return fail(GDC_E_OOM, cuda_msg("add: cudaMalloc", e));
@@ -452,8 +490,16 @@ class Batch final : public BatchIface {
   }
 
   // A slot that admit() gave out and whose state could not be written.
+  void member_free(void* p) {
+    if (!p) return;
+    if (member_pool(P.device))
+      cudaFreeAsync(p, stream);
+    else
+      cudaFree(p);
+  }
+
   void release(int slot) {
-    cudaFree(recs[slot].dmem);
+    member_free(recs[slot].dmem);
     recs[slot] = MemberRec();
   }
 
@@ -589,7 +635,8 @@ class Batch final : public BatchIface {
     int slot = -1;
     if (int rc = admit(N, M, dt, nsteps, cutoff, reserve, tmp_words * sizeof(double), &slot)) return rc;
     double* tmp = nullptr;
-    cudaError_t e = cudaMalloc(&tmp, tmp_words * sizeof(double));
+    cudaError_t e = member_pool(P.device) ? cudaMallocAsync((void**)&tmp, tmp_words * sizeof(double), stream)
+                                          : cudaMalloc(&tmp, tmp_words * sizeof(double));
     if (e != cudaSuccess) {
       cudaGetLastError();
       release(slot);
@@ -604,8 +651,8 @@ class Batch final : public BatchIface {
       rc = cudaMemcpyAsync(d_uvslot + slot, &lvl, sizeof(int), cudaMemcpyHostToDevice, stream) == cudaSuccess
                ? GDC_OK
                : GDC_E_CUDA;
+    member_free(tmp);
     e = cudaStreamSynchronize(stream);
-    cudaFree(tmp);
     if (rc != GDC_OK || e != cudaSuccess) {
       if (e == cudaSuccess) e = cudaGetLastError();
       release(slot);
@@ -802,7 +849,7 @@ class Batch final : public BatchIface {
     if (!valid(id)) return fail(GDC_E_CONFIG, "remove: unknown member");
     sync_stream();
     MemberRec& r = recs[id];
-    cudaFree(r.dmem);
+    member_free(r.dmem);
     r = MemberRec();
     std::memset(&hdesc[id], 0, sizeof(MemberDev<T>));
     dirty = true;
@@ -1430,8 +1477,8 @@ class Batch final : public BatchIface {
   void release() {
     if (stream) cudaStreamSynchronize(stream);
     invalidate_graphs();
-    for (auto& r : recs)
-      if (r.dmem) cudaFree(r.dmem);
+    for (auto& r : recs) member_free(r.dmem);
+    if (stream) cudaStreamSynchronize(stream);
     for (void* p : allocs) cudaFree(p);
     if (d_wl) cudaFree(d_wl);
     if (d_twl) cudaFree(d_twl);
@@ -2094,6 +2141,7 @@ int gdc_device_mem_info(int device, size_t* free_bytes, size_t* total_bytes) {
   if (cudaSetDevice(device) != cudaSuccess) return GDC_E_CUDA;
   size_t f = 0, t = 0;
   if (cudaMemGetInfo(&f, &t) != cudaSuccess) return GDC_E_CUDA;
+  f = gdc::free_device_memory(device);
   if (free_bytes) *free_bytes = f;
   if (total_bytes) *total_bytes = t;
   return GDC_OK;
