@@ -248,7 +248,11 @@ int gdc_device_mem_info(int device, size_t* free_bytes, size_t* total_bytes);
  * polar rows; each entry 0 <= c <= num_lon/2 - 1 (the reference's factor
  * rows hold 2 (c+1) <= num_lon entries, src/filter_mod.F90:79-96), else
  * GDC_E_CONFIG.  GDC_E_OOM when free device memory minus `reserve_bytes`
- * cannot hold it. */
+ * cannot hold it.  Member state comes from the device's default
+ * stream-ordered memory pool (cudaMallocAsync in the batch's stream); the
+ * library raises that pool's release threshold so that retired members'
+ * memory stays reserved for the next admission, and counts the pool's
+ * unused reserve as free (as gdc_device_mem_info does). */
 int gdc_batch_add(gdc_batch* b, int num_lon, int num_lat,
                   double time_step_size, long long nsteps, const int* cutoff,
                   const double* u, const double* v, const double* gd,
