@@ -301,12 +301,13 @@ def plain_fp64(gdc, torch, ts, steps=360):
     s64, s32 = out[gdc.FP64][1], out[gdc.FP32][1]
     return {"value": N * M * steps / (out[gdc.FP64][0] / 1e3), "ms": out[gdc.FP64][0],
             "fp32_value": N * M * steps / (out[gdc.FP32][0] / 1e3),
-            "l2_fp32_vs_fp64": {"gd": rl2(s32[2], s64[2]), "u": rl2(s32[0], s64[0]), "v": rl2(s32[1], s64[1])}}
+            "l2_fp32_vs_fp64": {"gd": rl2(s32[2], s64[2]), "u": rl2(s32[0], s64[0]), "v": rl2(s32[1], s64[1])},
+            "fp64_fma_gfma_per_s": gdc.fp64_fma_rate(0)}
 
 
 def stage_traffic():
     """DRAM bytes per stage launch from the committed ncu capture of this
-    workload (profiles/stage_kernel_f32_16x64_ensemble64.md)."""
+    workload (the .traffic.json beside its summary under profiles/)."""
     try:
         rec = json.loads((ROOT / "profiles" / "stage_kernel_f32_16x64_ensemble64.traffic.json").read_text())
         return rec["mean_dram_bytes_per_launch"]
@@ -646,7 +647,11 @@ def run_ours(args, rank, world, dist):
                        "config": "360x181 dt 240 s, 360 steps, FP64, one member",
                        "fp32_single_member_value": plain["fp32_value"],
                        "l2_fp32_vs_fp64_after_1_day": plain["l2_fp32_vs_fp64"],
-                       "batched_fp32_over_plain_fp64": value / plain["value"]},
+                       "batched_fp32_over_plain_fp64": value / plain["value"],
+                       # the plain path's roof is the FP64 unit, not HBM (the ncu
+                       # summary of its stage kernel: FP64 pipe 62-66 % busy)
+                       "fp64_roof": {"fma_rate_measured_gfma_per_s": plain["fp64_fma_gfma_per_s"],
+                                     "kernel": "an FMA-chain kernel on every SM (gdc_fp64_fma_rate)"}},
         "precision_720x361": precision,
         "serving": serving,
         "beside_path": beside,

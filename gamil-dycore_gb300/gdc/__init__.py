@@ -164,6 +164,7 @@ def lib() -> ctypes.CDLL:
             "gdc_batch_autotune": (ctypes.c_int, [vp, ip, ip, dp]),
             "gdc_batch_profile": (ctypes.c_int, [vp, ctypes.c_int, dp, i64p]),
             "gdc_algorithmic_bytes_per_gpt_step": (ctypes.c_double, [ctypes.POINTER(Params)]),
+            "gdc_fp64_fma_rate": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
             "gdc_tendency_noalloc": (ctypes.c_int, [ctypes.POINTER(Params), ctypes.c_int, vp, vp, vp, vp, vp, vp,
                                                     vp, vp, vp, vp]),
             "gdc_noalloc_last_error": (ctypes.c_char_p, []),
@@ -239,6 +240,15 @@ def steps_for_run(p: Params) -> int:
 
 def algorithmic_bytes_per_gpt_step(p: Params) -> float:
     return lib().gdc_algorithmic_bytes_per_gpt_step(ctypes.byref(p))
+
+
+def fp64_fma_rate(device: int = 0) -> float:
+    """The device's FP64 fused multiply-add rate, 1e9 FMA/s (the FP64 path's roof)."""
+    r = ctypes.c_double()
+    rc = lib().gdc_fp64_fma_rate(device, ctypes.byref(r))
+    if rc:
+        raise GdcError(rc, "gdc_fp64_fma_rate failed")
+    return r.value
 
 
 def member_bytes(p: Params, num_lon: int, num_lat: int) -> int:

@@ -368,6 +368,12 @@ int gdc_batch_profile(gdc_batch* b, int nsteps, double* ms, long long* launches)
  * model step) for this batch's scheme and precision. */
 double gdc_algorithmic_bytes_per_gpt_step(const gdc_params* scheme);
 
+/* No counterpart in the reference: the device's FP64 fused multiply-add
+ * rate in 1e9 FMA/s (an FMA-chain kernel on every SM, timed with CUDA
+ * events), the roof of the FP64 path, which is bound by that unit and not
+ * by memory. */
+int gdc_fp64_fma_rate(int device, double* gfma_per_s);
+
 #ifdef __cplusplus
 }
 #endif
