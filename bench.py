@@ -302,7 +302,7 @@ def plain_fp64(gdc, torch, ts, steps=360):
     return {"value": N * M * steps / (out[gdc.FP64][0] / 1e3), "ms": out[gdc.FP64][0],
             "fp32_value": N * M * steps / (out[gdc.FP32][0] / 1e3),
             "l2_fp32_vs_fp64": {"gd": rl2(s32[2], s64[2]), "u": rl2(s32[0], s64[0]), "v": rl2(s32[1], s64[1])},
-            "fp64_fma_gfma_per_s": gdc.fp64_fma_rate(0)}
+            "fp64_fma_gfma_per_s": gdc.fp64_fma_rate(torch.cuda.current_device())}
 
 
 def stage_traffic():

@@ -2,6 +2,8 @@
 // parameter defaults, the /dycore_params/ namelist reader, the run length,
 // the mesh and coefficient tables (FP64, evaluated exactly as the reference
 // evaluates them) and the initial-condition hooks.
+#include <cuda_runtime.h>
+
 #include "gdc_internal.h"
 
 #include <cctype>
@@ -142,7 +144,14 @@ extern "C" void gdc_params_default(gdc_params* p) {
   p->uv_adv_upwind_lat_beta = 0.5;         // :60
   p->use_zonal_tend_filter = 1;            // :65
   p->precision = GDC_FP64;
-  p->device = 0;
+  // the calling thread's current CUDA device (0 where there is none), as a
+  // process that runs one rank per device has selected it
+  int d = 0;
+  if (cudaGetDevice(&d) != cudaSuccess) {
+    cudaGetLastError();
+    d = 0;
+  }
+  p->device = d;
 }
 
 extern "C" int gdc_steps_for_run(const gdc_params* p) {

@@ -67,7 +67,7 @@ typedef struct gdc_params {
   int run_minutes;
   int run_seconds;
   int precision;
-  int device;
+  int device; /* CUDA device; gdc_params_default takes the calling thread's current one */
   /* Extension, not in the reference (0 = the reference's behaviour): the
    * s1/s2 rescale of a filtered tendency row (src/dycore_mod.F90:212-219)
    * is skipped -- the row is filtered but not rescaled -- when
