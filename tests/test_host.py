@@ -43,6 +43,10 @@ def test_defaults_follow_params_mod(native):
     p = gdc.default_params()
     assert p.subcycles == 4 and p.diffusion_order == 2 and p.uv_adv_upwind_lat_beta == 0.5
     assert p.use_zonal_tend_filter == 1 and p.uv_adv_scheme == gdc.ADV_CENTER_DIFF
+    # the calling thread's current CUDA device (0 without one)
+    import torch
+    expect = torch.cuda.current_device() if torch.cuda.is_available() else 0
+    assert p.device == expect
 
 
 def test_seeded_state_is_nondivergent(native):
