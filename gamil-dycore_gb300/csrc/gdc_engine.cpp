@@ -201,6 +201,7 @@ class HostPool {
 cudaMemPool_t member_pool(int device) {
   static std::mutex m;
   static std::vector<cudaMemPool_t> pools;
+  if (device < 0) return nullptr;
   std::lock_guard<std::mutex> g(m);
   if ((int)pools.size() <= device) pools.resize(device + 1, nullptr);
   if (!pools[device]) {
